@@ -1,0 +1,425 @@
+// Host orchestration and C ABI of the GB300 HSMU SpGEMM engine.
+//
+// Pipeline for C = A * B (reference: compressed_NHC_spgemm,
+// src/compressed/compressed_NHC_spgemm.cu:22-248):
+//   1. B -> 64-column bit tiles (k_tiles count, scan, fill)      [skipped with hsmu_spgemm_tiled]
+//   2. per-row bounds + row binning (k_bounds)
+//   3. exact symbolic count (k_count_ds / k_count_l)
+//   4. exclusive scan -> C row_ptr, nnz(C); ONE host read (8 bytes + flags)
+//      and the output allocation
+//   5a. sorted C columns + numeric windows (k_struct_ds / k_struct_l)
+//   5b. values (k_numeric)
+// The reference makes ~10 blocking host round trips and several cudaMalloc
+// calls inside its timed region; this engine makes one read of a small
+// control block and allocates from a stream-ordered pool that keeps freed
+// memory cached across calls.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/hsmu_gb.h"
+#include "hsmu_common.cuh"
+#include "hsmu_kernels.h"
+
+namespace hsmu {
+int configure_count();
+int configure_structure();
+int configure_numeric();
+}  // namespace hsmu
+
+using namespace hsmu;
+
+struct hsmu_handle_s {
+    int device;
+    int nsm;
+    Ctl *h_ctl;  // pinned host mirror of the control block
+    cudaEvent_t ev[8];
+};
+
+namespace {
+
+const char *kErr[] = {"ok",
+                      "invalid argument",
+                      "allocation failed",
+                      "CUDA error",
+                      "overflow: nnz(C) or a scratch size does not fit int32",
+                      "input CSR not canonical (columns must be strictly increasing and in range)",
+                      "internal consistency check failed on the device",
+                      "bounded device wait timed out",
+                      "no usable sm_103 device"};
+
+int from_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return HSMU_OK;
+    if (e == cudaErrorMemoryAllocation) return HSMU_ERR_ALLOC;
+    return HSMU_ERR_CUDA;
+}
+
+#define CK(x)                                \
+    do {                                     \
+        cudaError_t _e = (x);                \
+        if (_e != cudaSuccess) {             \
+            rc = from_cuda(_e);              \
+            goto done;                       \
+        }                                    \
+    } while (0)
+
+int err_from_dev(int err) {
+    if (!err) return HSMU_OK;
+    if (err & DERR_UNSORTED) return HSMU_ERR_UNSORTED;
+    if (err & DERR_OVERFLOW) return HSMU_ERR_OVERFLOW;
+    return HSMU_ERR_INTERNAL;
+}
+
+bool csr_ok(const hsmu_csr *X) {
+    if (!X || X->M < 0 || X->N < 0 || X->nnz < 0) return false;
+    if (!X->row_ptr) return false;
+    if (X->nnz > 0 && (!X->col || !X->val)) return false;
+    return true;
+}
+
+DevCSR dev(const hsmu_csr *X) { return DevCSR{X->M, X->N, (long long)X->nnz, X->row_ptr, X->col, X->val}; }
+
+template <class T>
+cudaError_t palloc(T **p, size_t n, cudaStream_t st) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMallocAsync(reinterpret_cast<void **>(p), n * sizeof(T), st);
+}
+
+template <class T>
+void pfree(T *&p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+}
+
+int grid_rows(const hsmu_handle_s *h) { return h->nsm * 8; }
+
+// B -> tiles into caller-visible arrays (tile arrays sized by nnz(B) >= tiles)
+int build_tiles(hsmu_handle_s *h, const hsmu_csr *B, hsmu_btiles *out, Ctl *ctl, int validate, cudaStream_t st,
+                bool read_count) {
+    int rc = HSMU_OK;
+    int *tcnt = nullptr, *scan_tmp = nullptr;
+    long long *tot = nullptr;
+    DevCSR Bd = dev(B);
+    out->M = B->M;
+    out->N = B->N;
+    out->ntiles = 0;
+    out->tile_ptr = nullptr;
+    out->tile_col = nullptr;
+    out->mask = nullptr;
+    out->tile_off = nullptr;
+    CK(palloc(&out->tile_ptr, (size_t)B->M + 1, st));
+    CK(palloc(&out->tile_col, (size_t)B->nnz, st));
+    CK(palloc(&out->mask, (size_t)B->nnz, st));
+    CK(palloc(&out->tile_off, (size_t)B->nnz, st));
+    CK(palloc(&tcnt, (size_t)B->M + 1, st));
+    CK(palloc(&scan_tmp, scan_tmp_ints(B->M), st));
+    CK(palloc(&tot, 1, st));
+    launch_tiles_count(Bd, tcnt, validate, ctl, grid_rows(h), st);
+    launch_scan(tcnt, out->tile_ptr, B->M, tot, scan_tmp, ctl, st);
+    launch_tiles_fill(Bd, out->tile_ptr, out->tile_col, reinterpret_cast<unsigned long long *>(out->mask), out->tile_off, ctl, grid_rows(h), st);
+    CK(cudaGetLastError());
+    if (read_count) {
+        CK(cudaMemcpyAsync(&ctl->ntiles, out->tile_ptr + B->M, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    }
+done:
+    pfree(tcnt, st);
+    pfree(scan_tmp, st);
+    pfree(tot, st);
+    if (rc != HSMU_OK) hsmu_btiles_free(out);
+    return rc;
+}
+
+int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hsmu_btiles *Bt_in, hsmu_csr *C,
+                const hsmu_opts *opts, cudaStream_t st, hsmu_stats *stats) {
+    if (!h || !csr_ok(A) || !csr_ok(B) || !C) return HSMU_ERR_INVALID;
+    if (A->N != B->M) return HSMU_ERR_INVALID;
+    if (Bt_in && (Bt_in->M != B->M || Bt_in->N != B->N || !Bt_in->tile_ptr)) return HSMU_ERR_INVALID;
+    hsmu_opts o{};
+    if (opts) o = *opts;
+    const int M = A->M;
+    int rc = HSMU_OK;
+    Ctl *ctl = nullptr;
+    hsmu_btiles bt{};
+    bool own_tiles = false;
+    RowInfo ri{};
+    int *scan_tmp = nullptr;
+    Window *win = nullptr;
+    long long win_cap = 0;
+    int *crp = nullptr, *ccol = nullptr;
+    double *cval = nullptr;
+    Ctl hc{};
+    DevCSR Ad = dev(A), Bd = dev(B);
+    DevTiles Btd{};
+    std::memset(C, 0, sizeof(*C));
+
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        cudaEventRecord(h->ev[0], st);
+    }
+    CK(palloc(&ctl, 1, st));
+    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    if (o.validate) {
+        // check both operands before any kernel indexes through them
+        launch_validate(Ad, ctl, grid_rows(h), st);
+        launch_validate(Bd, ctl, grid_rows(h), st);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (h->h_ctl->err) {
+            rc = err_from_dev(h->h_ctl->err);
+            goto done;
+        }
+    }
+
+    // 1. B tiles
+    if (Bt_in) {
+        bt = *Bt_in;
+    } else {
+        rc = build_tiles(h, B, &bt, ctl, 0, st, stats != nullptr);
+        if (rc) goto done;
+        own_tiles = true;
+    }
+    Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
+    if (stats) cudaEventRecord(h->ev[1], st);
+
+    // 2. bounds and bins
+    CK(palloc(&ri.prod, (size_t)M, st));
+    CK(palloc(&ri.tmin, (size_t)M, st));
+    CK(palloc(&ri.tmax, (size_t)M, st));
+    CK(palloc(&ri.bins, (size_t)M * NBIN, st));
+    CK(palloc(&ri.cnnz, (size_t)M + 1, st));
+    CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
+    CK(palloc(&crp, (size_t)M + 1, st));
+    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
+    // 3. exact count
+    launch_count(Ad, Btd, ri, ctl, h->nsm, st);
+    // 4. scan -> row_ptr, nnz
+    launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (stats) cudaEventRecord(h->ev[2], st);
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        goto done;
+    }
+    if (hc.nnz > INT_MAX) {
+        rc = HSMU_ERR_OVERFLOW;
+        goto done;
+    }
+    win_cap = (long long)hc.win_bound;
+    if (win_cap > INT_MAX) {
+        rc = HSMU_ERR_OVERFLOW;
+        goto done;
+    }
+    CK(palloc(&ccol, (size_t)hc.nnz, st));
+    CK(palloc(&cval, (size_t)hc.nnz, st));
+    CK(palloc(&win, (size_t)win_cap, st));
+    if (stats) cudaEventRecord(h->ev[3], st);
+
+    // 5a. structure + windows
+    if (hc.nnz > 0) launch_structure(Ad, Btd, ri, crp, ccol, win, win_cap, ctl, h->nsm, st);
+    if (stats) cudaEventRecord(h->ev[4], st);
+    // 5b. values
+    if (hc.nnz > 0) launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, ctl, o.arith, h->nsm, st);
+    CK(cudaGetLastError());
+    if (stats) cudaEventRecord(h->ev[5], st);
+
+    // completion + device-side checks
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        goto done;
+    }
+    C->M = M;
+    C->N = B->N;
+    C->nnz = (int32_t)hc.nnz;
+    C->owned = 1;
+    C->row_ptr = crp;
+    C->col = ccol;
+    C->val = cval;
+    crp = nullptr;
+    ccol = nullptr;
+    cval = nullptr;
+    if (stats) {
+        float t;
+        stats->products = hc.products;
+        stats->nnz_c = hc.nnz;
+        stats->ntiles_b = Bt_in ? Bt_in->ntiles : hc.ntiles;
+        stats->windows = hc.win_count;
+        cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
+        stats->ms_convert = t;
+        cudaEventElapsedTime(&t, h->ev[1], h->ev[2]);
+        stats->ms_symbolic = t;
+        cudaEventElapsedTime(&t, h->ev[2], h->ev[3]);
+        stats->ms_alloc = t;
+        cudaEventElapsedTime(&t, h->ev[3], h->ev[4]);
+        stats->ms_structure = t;
+        cudaEventElapsedTime(&t, h->ev[4], h->ev[5]);
+        stats->ms_numeric = t;
+        cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
+        stats->ms_total = t;
+    }
+done:
+    pfree(ctl, st);
+    if (own_tiles) {
+        pfree(bt.tile_ptr, st);
+        pfree(bt.tile_col, st);
+        pfree(bt.mask, st);
+        pfree(bt.tile_off, st);
+    }
+    pfree(ri.prod, st);
+    pfree(ri.tmin, st);
+    pfree(ri.tmax, st);
+    pfree(ri.bins, st);
+    pfree(ri.cnnz, st);
+    pfree(scan_tmp, st);
+    pfree(win, st);
+    pfree(crp, st);
+    pfree(ccol, st);
+    pfree(cval, st);
+    if (rc != HSMU_OK) cudaStreamSynchronize(st);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hsmu_strerror(int status) {
+    if (status < 0 || status >= (int)(sizeof(kErr) / sizeof(kErr[0]))) return "unknown status";
+    return kErr[status];
+}
+
+int hsmu_abi_version(void) { return HSMU_ABI_VERSION; }
+
+int hsmu_handle_create(hsmu_handle *out) {
+    if (!out) return HSMU_ERR_INVALID;
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return HSMU_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return HSMU_ERR_NO_DEVICE;
+    if (prop.major < 10) return HSMU_ERR_NO_DEVICE;
+    hsmu_handle_s *h = new (std::nothrow) hsmu_handle_s();
+    if (!h) return HSMU_ERR_ALLOC;
+    h->device = dev;
+    h->nsm = prop.multiProcessorCount;
+    if (cudaMallocHost(reinterpret_cast<void **>(&h->h_ctl), sizeof(Ctl)) != cudaSuccess) {
+        delete h;
+        return HSMU_ERR_ALLOC;
+    }
+    for (auto &e : h->ev) cudaEventCreate(&e);
+    // keep freed pool memory cached between calls (no re-mapping of large outputs)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    int e = configure_count();
+    if (!e) e = configure_structure();
+    if (!e) e = configure_numeric();
+    if (e) {
+        hsmu_handle_destroy(h);
+        return HSMU_ERR_CUDA;
+    }
+    *out = h;
+    return HSMU_OK;
+}
+
+int hsmu_handle_destroy(hsmu_handle h) {
+    if (!h) return HSMU_OK;
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->h_ctl) cudaFreeHost(h->h_ctl);
+    delete h;
+    return HSMU_OK;
+}
+
+int hsmu_spgemm(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_opts *opts,
+                void *stream, hsmu_stats *stats) {
+    return spgemm_impl(h, A, B, nullptr, C, opts, static_cast<cudaStream_t>(stream), stats);
+}
+
+int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, const hsmu_btiles *Bt, hsmu_csr *C,
+                      const hsmu_opts *opts, void *stream, hsmu_stats *stats) {
+    if (!Bt) return HSMU_ERR_INVALID;
+    return spgemm_impl(h, A, B, Bt, C, opts, static_cast<cudaStream_t>(stream), stats);
+}
+
+int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream) {
+    if (!h || !csr_ok(B) || !out) return HSMU_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = HSMU_OK;
+    Ctl *ctl = nullptr;
+    Ctl hc{};
+    std::memset(out, 0, sizeof(*out));
+    CK(palloc(&ctl, 1, st));
+    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    launch_validate(dev(B), ctl, grid_rows(h), st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h->h_ctl->err) {
+        rc = err_from_dev(h->h_ctl->err);
+        goto done;
+    }
+    rc = build_tiles(h, B, out, ctl, 0, st, true);
+    if (rc) goto done;
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        hsmu_btiles_free(out);
+        goto done;
+    }
+    out->ntiles = hc.ntiles;
+done:
+    pfree(ctl, st);
+    return rc;
+}
+
+int hsmu_btiles_free(hsmu_btiles *t) {
+    if (!t) return HSMU_ERR_INVALID;
+    cudaFree(t->tile_ptr);
+    cudaFree(t->tile_col);
+    cudaFree(t->mask);
+    cudaFree(t->tile_off);
+    std::memset(t, 0, sizeof(*t));
+    return HSMU_OK;
+}
+
+int hsmu_csr_free(hsmu_csr *C) {
+    if (!C) return HSMU_ERR_INVALID;
+    if (C->owned) {
+        cudaFree(C->row_ptr);
+        cudaFree(C->col);
+        cudaFree(C->val);
+    }
+    std::memset(C, 0, sizeof(*C));
+    return HSMU_OK;
+}
+
+int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream) {
+    if (!csr_ok(C) || !row_ptr || (C->nnz > 0 && (!col || !val))) return HSMU_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = HSMU_OK;
+    CK(cudaMemcpyAsync(row_ptr, C->row_ptr, sizeof(int32_t) * ((size_t)C->M + 1), cudaMemcpyDeviceToHost, st));
+    if (C->nnz > 0) {
+        CK(cudaMemcpyAsync(col, C->col, sizeof(int32_t) * (size_t)C->nnz, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(val, C->val, sizeof(double) * (size_t)C->nnz, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+done:
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// Warp- and block-level helpers shared by the symbolic, structure and
+// numeric kernels: the flattened walk over the (A entry, B segment) pairs of
+// one row, and block scans.
+#pragma once
+#include "hsmu_common.cuh"
+
+namespace hsmu {
+
+// Index of the segment that owns flat item g, given the inclusive prefix
+// `incl` of 32 segment lengths held one per lane (non-decreasing): the number
+// of lanes whose incl <= g.  All 32 lanes must call it (5 indexed shuffles).
+__device__ __forceinline__ int seg_of(int incl, int g) {
+    int s = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const int v = __shfl_sync(FULL, incl, s + step - 1);
+        if (v <= g) s += step;
+    }
+    return s;
+}
+
+// Visit every B tile of the rows referenced by A entries [a_lo, a_hi), with
+// the tile range of each B row optionally restricted to tile ids [c0, c1)
+// (restrict = true: lower_bound on the sorted tile ids).  Lanes take 32
+// consecutive flat items at a time, so every lane is busy regardless of the
+// B row lengths.  fn(tile_index) is called for valid items only.  The walk
+// starts at A entry a_lo + first and advances `stride` entries per step
+// (first/stride let several warps of a CTA share one row).
+template <bool RESTRICT, class Fn>
+__device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, int stride,
+                                                const int *__restrict__ acol, const int *__restrict__ tptr,
+                                                const int *__restrict__ tcol, int c0, int c1, Fn fn) {
+    const int lane = lane_id();
+    for (int pb = a_lo + first; pb < a_hi; pb += stride) {
+        const int p = pb + lane;
+        int lo = 0, hi = 0;
+        if (p < a_hi) {
+            const int k = __ldg(acol + p);
+            lo = __ldg(tptr + k);
+            hi = __ldg(tptr + k + 1);
+            if (RESTRICT) {
+                lo = lower_bound_i32(tcol, lo, hi, c0);
+                hi = lower_bound_i32(tcol, lo, hi, c1);
+            }
+        }
+        const int len = hi - lo;
+        const int incl = warp_incl_scan(len);
+        const int total = __shfl_sync(FULL, incl, WARP - 1);
+        const int excl = incl - len;
+        for (int f = 0; f < total; f += WARP) {
+            const int g = f + lane;
+            const int s = seg_of(incl, g);
+            const int idx = __shfl_sync(FULL, lo, s) + (g - __shfl_sync(FULL, excl, s));
+            if (g < total) fn(idx);
+        }
+    }
+}
+
+// Block-wide exclusive scans over one value per thread (blockDim.x == NT).
+// s_tmp needs NT/32 + 1 entries.  Contains __syncthreads.
+template <int NT, class T>
+__device__ __forceinline__ T block_excl_sum(T v, T *s_tmp, T &total) {
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    T incl = warp_incl_scan(v);
+    if (lane == 31) s_tmp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        T x = lane < (NT / 32) ? s_tmp[lane] : T(0);
+        T xi = warp_incl_scan(x);
+        if (lane < (NT / 32)) s_tmp[lane] = xi - x;
+        if (lane == 31) s_tmp[NT / 32] = xi;
+    }
+    __syncthreads();
+    total = s_tmp[NT / 32];
+    T r = incl - v + s_tmp[w];
+    __syncthreads();
+    return r;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_incl_max(T v) {
+    const int lane = lane_id();
+#pragma unroll
+    for (int d = 1; d < WARP; d <<= 1) {
+        T o = __shfl_up_sync(FULL, v, d);
+        if (lane >= d) v = max(v, o);
+    }
+    return v;
+}
+
+// exclusive max-scan; threads before the first contribute `ident`
+template <int NT, class T>
+__device__ __forceinline__ T block_excl_max(T v, T *s_tmp, T ident) {
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    T incl = warp_incl_max(v);
+    T ex = __shfl_up_sync(FULL, incl, 1);
+    if (lane == 0) ex = ident;
+    if (lane == 31) s_tmp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        T x = lane < (NT / 32) ? s_tmp[lane] : ident;
+        T xi = warp_incl_max(x);
+        T xe = __shfl_up_sync(FULL, xi, 1);
+        if (lane == 0) xe = ident;
+        if (lane < (NT / 32)) s_tmp[lane] = xe;
+    }
+    __syncthreads();
+    T r = max(ex, s_tmp[w]);
+    __syncthreads();
+    return r;
+}
+
+}  // namespace hsmu

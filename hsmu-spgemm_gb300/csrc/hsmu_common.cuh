@@ -1,0 +1,110 @@
+// Shared definitions for the GB300 HSMU SpGEMM kernels (sm_103a).
+//
+// Data layout in HBM (all arrays are plain device allocations):
+//   A, B, C   int32 row_ptr / col, FP64 val (canonical CSR, sorted columns)
+//   B tiles   tile_ptr[K+1], tile_col[T], mask[T] (u64), tile_off[T]
+//   rows      per A row: products (i64), tile bound (i64), first/last C tile
+//   bins      NBIN slabs of M row ids (row classes for the symbolic and
+//             structure kernels)
+//   windows   numeric work items {row, first slot, slot count, first tile}
+//   ctl       one small control block of counters / totals / error bits
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hsmu {
+
+constexpr int WARP = 32;
+constexpr unsigned FULL = 0xffffffffu;
+
+// A C row (or numeric window) whose tile span is at most SPAN_T tiles is
+// handled by one warp with a dense per-tile table in shared memory.
+constexpr int SPAN_T = 512;
+// Maximum slots (C entries) of one numeric window; windows are cut at tile
+// boundaries whose slot base crosses a multiple of WIN_CUT, so a window holds
+// at most WIN_CUT + 63 < WIN_CAP slots.
+constexpr int WIN_CAP = 1024;
+constexpr int WIN_CUT = WIN_CAP - 64;
+// Tiles per chunk of the CTA (large-row) kernels.
+constexpr int DCH_COUNT = 8192;   // count pass: 8 B per tile  -> 64 KB
+constexpr int DCH_STRUCT = 8192;  // structure pass: 12 B per tile -> 96 KB
+
+// Row classes
+enum RowBin : int {
+    BIN_DS = 0,   // tile span <= SPAN_T : one warp, dense span table
+    BIN_L = 1,    // wider rows          : one CTA, dense chunked table
+    NBIN = 2
+};
+
+// device error bits (ctl->err)
+enum DevErr : int {
+    DERR_UNSORTED = 1,
+    DERR_INTERNAL = 2,
+    DERR_CAPACITY = 4,
+    DERR_OVERFLOW = 8
+};
+
+struct Window {
+    int row;   // C row
+    int s0;    // absolute index of the first slot (C entry) of the window
+    int cnt;   // number of slots
+    int t0;    // tile id of the first slot's column
+};
+
+struct Ctl {
+    unsigned long long products;     // sum of intermediate products
+    unsigned long long win_bound;    // upper bound on the number of windows
+    long long nnz;                   // exact nnz(C) (after the scan)
+    int bin_count[NBIN];
+    int win_count;                   // windows emitted by the structure pass
+    int win_next;                    // dynamic work counter of the numeric pass
+    int err;
+    int ntiles;                      // B tiles (after the B conversion scan)
+    int pad[2];
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & (WARP - 1); }
+
+template <class T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
+    const int lane = lane_id();
+#pragma unroll
+    for (int d = 1; d < WARP; d <<= 1) {
+        T o = __shfl_up_sync(FULL, v, d);
+        if (lane >= d) v += o;
+    }
+    return v;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(FULL, v, d);
+    return v;
+}
+
+__device__ __forceinline__ int popc64(unsigned long long x) { return __popcll(x); }
+
+// number of set bits of m strictly below bit b (0 <= b < 64)
+__device__ __forceinline__ int rank64(unsigned long long m, int b) {
+    return __popcll(m & ((1ull << b) - 1ull));
+}
+
+// first index in [lo, hi) with a[idx] >= key (a sorted ascending)
+__device__ __forceinline__ int lower_bound_i32(const int *__restrict__ a, int lo, int hi, int key) {
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void set_err(int *err, int bit) { atomicOr(err, bit); }
+
+}  // namespace hsmu

@@ -1,0 +1,192 @@
+// Stage 2: per-row bounds + row binning, and the device exclusive scan.
+//
+// Bounds: for every A row, the number of intermediate products
+// sum_{k in A(i,:)} nnz(B(k,:)) (64-bit; the reference counts it on the host,
+// src/NHC_spgemm.cuh:37-42, and bounds C tiles per row with k_compute_flop,
+// src/small/mask.cuh:14-51) and the exact first/last C tile of the row (the
+// min/max over the first/last tile of every referenced B row, which are at
+// the ends of B's sorted tile lists).  The tile span decides the row class
+// (one warp with a dense span table, or one CTA with a chunked table), which
+// replaces the reference's host-round-trip binning (src/bining.cuh:1-207):
+// rows are binned on the device with block-aggregated atomics.
+//
+// Scan: three launches (block sums, scan of block sums, block scans), 64-bit
+// running totals, int32 output; replaces cub::DeviceScan::ExclusiveSum plus
+// the full-array D2H copies of the reference
+// (src/compressed/compressed_tileOR.cuh:620-622).
+#include <climits>
+
+#include "hsmu_common.cuh"
+#include "hsmu_kernels.h"
+
+namespace hsmu {
+
+template <int G>
+__global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ arp, const int *__restrict__ acol,
+                                                const int *__restrict__ brp, const int *__restrict__ tptr,
+                                                const int *__restrict__ tcol, int N, RowInfo ri, Ctl *ctl) {
+    constexpr int RPB = 256 / G;  // rows per block iteration
+    __shared__ int s_cnt[NBIN];
+    __shared__ int s_base[NBIN];
+    const int sub = threadIdx.x & (G - 1);
+    const int rloc = threadIdx.x / G;
+    unsigned long long my_prod = 0, my_wb = 0;
+    if (threadIdx.x < NBIN) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int rb = blockIdx.x * RPB; rb < M; rb += gridDim.x * RPB) {
+        const int i = rb + rloc;
+        long long prod = 0;
+        int tmin = INT_MAX, tmax = -1;
+        if (i < M) {
+            for (int p = arp[i] + sub; p < arp[i + 1]; p += G) {
+                const int k = __ldg(acol + p);
+                prod += __ldg(brp + k + 1) - __ldg(brp + k);
+                const int t0 = __ldg(tptr + k), t1 = __ldg(tptr + k + 1);
+                if (t1 > t0) {
+                    tmin = min(tmin, __ldg(tcol + t0));
+                    tmax = max(tmax, __ldg(tcol + t1 - 1));
+                }
+            }
+        }
+#pragma unroll
+        for (int d = G / 2; d > 0; d >>= 1) {
+            prod += __shfl_xor_sync(FULL, prod, d, G);
+            tmin = min(tmin, __shfl_xor_sync(FULL, tmin, d, G));
+            tmax = max(tmax, __shfl_xor_sync(FULL, tmax, d, G));
+        }
+        int bin = -1, lpos = 0;
+        if (i < M && sub == 0) {
+            ri.prod[i] = prod;
+            ri.tmin[i] = tmin;
+            ri.tmax[i] = tmax;
+            if (prod == 0) {
+                ri.cnnz[i] = 0;
+            } else {
+                const int span = tmax - tmin + 1;
+                bin = span <= SPAN_T ? BIN_DS : BIN_L;
+                lpos = atomicAdd(&s_cnt[bin], 1);
+                my_prod += (unsigned long long)prod;
+                const long long cap = prod < (long long)N ? prod : (long long)N;
+                my_wb += (unsigned long long)(cap / WIN_CUT + (span - 1) / SPAN_T + 1);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < NBIN) {
+            s_base[threadIdx.x] = s_cnt[threadIdx.x] ? atomicAdd(&ctl->bin_count[threadIdx.x], s_cnt[threadIdx.x]) : 0;
+            s_cnt[threadIdx.x] = 0;
+        }
+        __syncthreads();
+        if (bin >= 0) ri.bins[(size_t)bin * M + s_base[bin] + lpos] = i;
+        __syncthreads();
+    }
+    my_prod = warp_sum(my_prod);
+    my_wb = warp_sum(my_wb);
+    if (lane_id() == 0) {
+        if (my_prod) atomicAdd(&ctl->products, my_prod);
+        if (my_wb) atomicAdd(&ctl->win_bound, my_wb);
+    }
+}
+
+void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int grid,
+                   cudaStream_t st) {
+    const double avg = A.M ? (double)A.nnz / A.M : 0.0;
+    if (avg <= 6)
+        k_bounds<4><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+    else if (avg <= 12)
+        k_bounds<8><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+    else if (avg <= 24)
+        k_bounds<16><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+    else
+        k_bounds<32><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+}
+
+// ---------------------------------------------------------------- scan
+constexpr int SCAN_T = 256;
+constexpr int SCAN_IPT = 8;
+constexpr int SCAN_ITEMS = SCAN_T * SCAN_IPT;
+
+// exclusive block scan of one long long per thread; returns block total
+__device__ __forceinline__ long long block_excl_scan(long long v, long long *s_warp, long long &total) {
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    long long incl = warp_incl_scan(v);
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        long long x = lane < (SCAN_T / 32) ? s_warp[lane] : 0;
+        long long xi = warp_incl_scan(x);
+        if (lane < (SCAN_T / 32)) s_warp[lane] = xi - x;
+        if (lane == 31) s_warp[SCAN_T / 32] = xi;
+    }
+    __syncthreads();
+    total = s_warp[SCAN_T / 32];
+    long long r = incl - v + s_warp[w];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_sums(const int *__restrict__ in, int n, long long *bsum) {
+    __shared__ long long s_warp[SCAN_T / 32 + 1];
+    const long long base = (long long)blockIdx.x * SCAN_ITEMS + threadIdx.x * SCAN_IPT;
+    long long v = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; j++)
+        if (base + j < n) v += in[base + j];
+    long long tot;
+    block_excl_scan(v, s_warp, tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_top(long long *bsum, int nb, long long *total64) {
+    __shared__ long long s_warp[SCAN_T / 32 + 1];
+    long long carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += SCAN_T) {
+        const int b = b0 + threadIdx.x;
+        long long v = b < nb ? bsum[b] : 0;
+        long long tot;
+        long long ex = block_excl_scan(v, s_warp, tot);
+        if (b < nb) bsum[b] = ex + carry;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) *total64 = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_out(const int *__restrict__ in, int *__restrict__ out, int n,
+                                                     const long long *__restrict__ boff, const long long *total64,
+                                                     Ctl *ctl) {
+    __shared__ long long s_warp[SCAN_T / 32 + 1];
+    const long long base = (long long)blockIdx.x * SCAN_ITEMS + threadIdx.x * SCAN_IPT;
+    int vals[SCAN_IPT];
+    long long v = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; j++) {
+        vals[j] = base + j < n ? in[base + j] : 0;
+        v += vals[j];
+    }
+    long long tot;
+    long long ex = block_excl_scan(v, s_warp, tot) + boff[blockIdx.x];
+    const bool ovf = *total64 > (long long)INT_MAX;
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; j++) {
+        if (base + j < n) out[base + j] = ovf ? 0 : (int)ex;
+        ex += vals[j];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        out[n] = ovf ? 0 : (int)*total64;
+        if (ovf) set_err(&ctl->err, DERR_OVERFLOW);
+    }
+}
+
+size_t scan_tmp_ints(int n) {
+    const int nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
+    return (size_t)(nb > 0 ? nb : 1) * 2 + 2;
+}
+
+void launch_scan(const int *in, int *out, int n, long long *total64, int *tmp, Ctl *ctl, cudaStream_t st) {
+    const int nb = n > 0 ? (n + SCAN_ITEMS - 1) / SCAN_ITEMS : 1;
+    long long *bsum = reinterpret_cast<long long *>(tmp);
+    k_scan_sums<<<nb, SCAN_T, 0, st>>>(in, n, bsum);
+    k_scan_top<<<1, SCAN_T, 0, st>>>(bsum, nb, total64);
+    k_scan_out<<<nb, SCAN_T, 0, st>>>(in, out, n, bsum, total64, ctl);
+}
+
+}  // namespace hsmu

@@ -1,0 +1,282 @@
+// Stage 5a: C column structure and numeric work items (windows).
+//
+// GB300 counterpart of h_get_Ccol_from_Ctile / k_formccol_shared_for_many_rows
+// (src/compressed/compressed_Ccol_symbolic.cuh:1-63,119-389), which expands
+// each C tile mask into columns with __ffsll and then rank-sorts every row in
+// O(n^2).  Here the row's tiles are rebuilt in a dense per-tile table
+// indexed by tile id, so they are already in column order: an exclusive scan
+// of the tile popcounts gives every tile's first slot and the columns are
+// written sorted, with no sort at all.
+//
+// The same pass cuts every row into numeric windows: consecutive tiles whose
+// first slot lies in the same WIN_CUT-slot block and whose tile ids lie in the
+// same SPAN_T-tile block.  A window therefore holds < WIN_CAP slots and spans
+// <= SPAN_T tiles, which bounds the numeric kernel's shared memory, and long
+// rows are split across many warps and SMs (the reference sends rows with
+// more than 4096 nnz to one CTA of the spECK dense accumulator,
+// src/compressed/compressed_Cval.cuh:300-365).
+#include "hsmu_block.cuh"
+#include "hsmu_kernels.h"
+
+namespace hsmu {
+
+constexpr int SDS_WARPS = 8;
+constexpr int SDS_WL = 64;  // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
+
+struct SdsSmem {
+    unsigned long long msk[SPAN_T];
+    int base[SPAN_T];
+    int wl[SDS_WL];
+    int wt[SDS_WL];
+};
+
+__global__ void __launch_bounds__(SDS_WARPS * 32) k_struct_ds(int M, const int *__restrict__ arp,
+                                                              const int *__restrict__ acol,
+                                                              const int *__restrict__ tptr,
+                                                              const int *__restrict__ tcol,
+                                                              const unsigned long long *__restrict__ tmask,
+                                                              RowInfo ri, const int *__restrict__ crp,
+                                                              int *__restrict__ ccol, Window *__restrict__ win,
+                                                              long long win_cap, Ctl *ctl) {
+    extern __shared__ unsigned long long s_dyn[];
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    SdsSmem &S = reinterpret_cast<SdsSmem *>(s_dyn)[w];
+    const int n = ctl->bin_count[BIN_DS];
+    const int *rows = ri.bins + (size_t)BIN_DS * M;
+    for (int r = blockIdx.x * SDS_WARPS + w; r < n; r += gridDim.x * SDS_WARPS) {
+        const int i = rows[r];
+        const int t0 = ri.tmin[i];
+        const int span = ri.tmax[i] - t0 + 1;
+        const int rowbase = crp[i];
+        const int nnz = crp[i + 1] - rowbase;
+        for (int t = lane; t < span; t += WARP) S.msk[t] = 0ull;
+        __syncwarp();
+        bool bad = false;
+        warp_walk_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, 0, 0, [&](int idx) {
+            const int t = __ldg(tcol + idx) - t0;
+            if (t >= 0 && t < span) atomicOr(&S.msk[t], __ldg(tmask + idx));
+            else bad = true;
+        });
+        if (__any_sync(FULL, bad)) {
+            if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
+            __syncwarp();
+            continue;
+        }
+        __syncwarp();
+        const int per = (span + WARP - 1) / WARP;
+        const int lo = min(span, lane * per), hi = min(span, lo + per);
+        int sum = 0;
+        for (int t = lo; t < hi; t++) sum += popc64(S.msk[t]);
+        const int incl = warp_incl_scan(sum);
+        const int total = __shfl_sync(FULL, incl, WARP - 1);
+        if (total != nnz) {
+            if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
+            __syncwarp();
+            continue;
+        }
+        int run = incl - sum;
+        int lastkey = -1;
+        for (int t = lo; t < hi; t++) {
+            const unsigned long long m = S.msk[t];
+            if (m) {
+                S.base[t] = run;
+                lastkey = run / WIN_CUT;
+                run += popc64(m);
+            }
+        }
+        int carry = __shfl_up_sync(FULL, warp_incl_max(lastkey), 1);
+        if (lane == 0) carry = -1;
+        int nst = 0;
+        {
+            int kk = carry;
+            for (int t = lo; t < hi; t++)
+                if (S.msk[t]) {
+                    const int key = S.base[t] / WIN_CUT;
+                    if (key != kk) nst++;
+                    kk = key;
+                }
+        }
+        const int st_incl = warp_incl_scan(nst);
+        const int nwin = __shfl_sync(FULL, st_incl, WARP - 1);
+        {
+            int pos = st_incl - nst, kk = carry;
+            for (int t = lo; t < hi; t++)
+                if (S.msk[t]) {
+                    const int key = S.base[t] / WIN_CUT;
+                    if (key != kk) {
+                        S.wl[pos] = S.base[t];
+                        S.wt[pos] = t;
+                        pos++;
+                    }
+                    kk = key;
+                }
+        }
+        __syncwarp();
+        int wbase = 0;
+        if (lane == 0) wbase = atomicAdd(&ctl->win_count, nwin);
+        wbase = __shfl_sync(FULL, wbase, 0);
+        if ((long long)wbase + nwin > win_cap) {
+            if (lane == 0) set_err(&ctl->err, DERR_CAPACITY);
+        } else {
+            for (int j = lane; j < nwin; j += WARP) {
+                const int s0 = S.wl[j];
+                const int e = (j + 1 < nwin) ? S.wl[j + 1] : total;
+                win[wbase + j] = Window{i, rowbase + s0, e - s0, t0 + S.wt[j]};
+            }
+        }
+        for (int t = lo; t < hi; t++) {
+            unsigned long long m = S.msk[t];
+            if (m) {
+                int pos = rowbase + S.base[t];
+                const int cb = (t0 + t) << 6;
+                while (m) {
+                    ccol[pos++] = cb + (__ffsll((long long)m) - 1);
+                    m &= m - 1ull;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+constexpr int SL_THREADS = 256;
+constexpr int SL_WL = 1024;  // > max windows in one chunk (DCH*64/WIN_CUT + DCH/SPAN_T + 1)
+constexpr int SL_PER = DCH_STRUCT / SL_THREADS;
+static_assert(DCH_STRUCT % SPAN_T == 0, "chunks must start on span-block boundaries");
+
+struct SlSmem {
+    unsigned long long msk[DCH_STRUCT];
+    int base[DCH_STRUCT];
+    int wl[SL_WL];
+    int wt[SL_WL];
+};
+
+__global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__restrict__ arp,
+                                                         const int *__restrict__ acol,
+                                                         const int *__restrict__ tptr,
+                                                         const int *__restrict__ tcol,
+                                                         const unsigned long long *__restrict__ tmask, RowInfo ri,
+                                                         const int *__restrict__ crp, int *__restrict__ ccol,
+                                                         Window *__restrict__ win, long long win_cap, Ctl *ctl) {
+    extern __shared__ unsigned long long s_dyn[];
+    SlSmem &S = *reinterpret_cast<SlSmem *>(s_dyn);
+    __shared__ int s_tmp[SL_THREADS / 32 + 1];
+    __shared__ int s_wbase;
+    constexpr int NWARP = SL_THREADS / 32;
+    const int w = threadIdx.x >> 5;
+    const int n = ctl->bin_count[BIN_L];
+    const int *rows = ri.bins + (size_t)BIN_L * M;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const int i = rows[r];
+        const int tmin = ri.tmin[i], tmax = ri.tmax[i];
+        const int a_lo = arp[i], a_hi = arp[i + 1];
+        const int rowbase = crp[i];
+        const int nnz = crp[i + 1] - rowbase;
+        const bool one_chunk = (tmax - tmin + 1) <= DCH_STRUCT;
+        int run_row = 0;
+        for (int c0 = tmin; c0 <= tmax; c0 += DCH_STRUCT) {
+            const int c1 = min(c0 + DCH_STRUCT, tmax + 1);
+            const int len = c1 - c0;
+            for (int t = threadIdx.x; t < len; t += SL_THREADS) S.msk[t] = 0ull;
+            __syncthreads();
+            bool bad = false;
+            auto orfn = [&](int idx) {
+                const int t = __ldg(tcol + idx) - c0;
+                if (t >= 0 && t < len) atomicOr(&S.msk[t], __ldg(tmask + idx));
+                else bad = true;
+            };
+            if (one_chunk)
+                warp_walk_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+            else
+                warp_walk_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+            if (bad) set_err(&ctl->err, DERR_INTERNAL);
+            __syncthreads();
+            const int lo = min(len, (int)threadIdx.x * SL_PER), hi = min(len, lo + SL_PER);
+            int sum = 0;
+            for (int t = lo; t < hi; t++) sum += popc64(S.msk[t]);
+            int chunk_total;
+            int run = block_excl_sum<SL_THREADS>(sum, s_tmp, chunk_total) + run_row;
+            int lastkey = -1;
+            for (int t = lo; t < hi; t++) {
+                const unsigned long long m = S.msk[t];
+                if (m) {
+                    S.base[t] = run;
+                    lastkey = (run / WIN_CUT) * 64 + t / SPAN_T;
+                    run += popc64(m);
+                }
+            }
+            const int carry = block_excl_max<SL_THREADS>(lastkey, s_tmp, -1);
+            int nst = 0;
+            {
+                int kk = carry;
+                for (int t = lo; t < hi; t++)
+                    if (S.msk[t]) {
+                        const int key = (S.base[t] / WIN_CUT) * 64 + t / SPAN_T;
+                        if (key != kk) nst++;
+                        kk = key;
+                    }
+            }
+            int nwin;
+            int pos = block_excl_sum<SL_THREADS>(nst, s_tmp, nwin);
+            {
+                int kk = carry;
+                for (int t = lo; t < hi; t++)
+                    if (S.msk[t]) {
+                        const int key = (S.base[t] / WIN_CUT) * 64 + t / SPAN_T;
+                        if (key != kk) {
+                            if (pos < SL_WL) {
+                                S.wl[pos] = S.base[t];
+                                S.wt[pos] = t;
+                            }
+                            pos++;
+                        }
+                        kk = key;
+                    }
+            }
+            if (threadIdx.x == 0) s_wbase = (nwin <= SL_WL) ? atomicAdd(&ctl->win_count, nwin) : -1;
+            __syncthreads();
+            const int wbase = s_wbase;
+            const int chunk_end = run_row + chunk_total;
+            if (wbase < 0 || (long long)wbase + nwin > win_cap || chunk_end > nnz) {
+                if (threadIdx.x == 0) set_err(&ctl->err, wbase < 0 || chunk_end <= nnz ? DERR_CAPACITY : DERR_INTERNAL);
+            } else {
+                for (int j = threadIdx.x; j < nwin; j += SL_THREADS) {
+                    const int s0 = S.wl[j];
+                    const int e = (j + 1 < nwin) ? S.wl[j + 1] : chunk_end;
+                    win[wbase + j] = Window{i, rowbase + s0, e - s0, c0 + S.wt[j]};
+                }
+                for (int t = lo; t < hi; t++) {
+                    unsigned long long m = S.msk[t];
+                    if (m) {
+                        int p = rowbase + S.base[t];
+                        const int cb = (c0 + t) << 6;
+                        while (m) {
+                            ccol[p++] = cb + (__ffsll((long long)m) - 1);
+                            m &= m - 1ull;
+                        }
+                    }
+                }
+            }
+            run_row = chunk_end;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0 && run_row != nnz) set_err(&ctl->err, DERR_INTERNAL);
+    }
+}
+
+void launch_structure(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol, Window *win,
+                      long long win_cap, Ctl *ctl, int nsm, cudaStream_t st) {
+    k_struct_ds<<<nsm * 4, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
+        A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol, win, win_cap, ctl);
+    k_struct_l<<<nsm * 2, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol,
+                                                            win, win_cap, ctl);
+}
+
+int configure_structure() {
+    int e = (int)cudaFuncSetAttribute(k_struct_ds, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SDS_WARPS * (int)sizeof(SdsSmem));
+    if (e) return e;
+    return (int)cudaFuncSetAttribute(k_struct_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SlSmem));
+}
+
+}  // namespace hsmu

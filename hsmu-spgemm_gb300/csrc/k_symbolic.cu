@@ -1,0 +1,121 @@
+// Stage 3: exact symbolic count, nnz(C(i,:)) for every row.
+//
+// GB300 counterpart of the reference's two symbolic passes
+// (k_tilePtr_symbolic_* in src/compressed/compressed_tilePtr_symbolic.cuh:174-496,
+// which count C tiles with a shared-memory hash, and k_tileOR_* in
+// src/compressed/compressed_tileOR.cuh:19-337, which OR the u64 B tile masks
+// into those tiles and sum their popcounts).  Both are folded into one pass:
+// the row's C tiles are ORed into a dense per-tile table indexed by
+// (tile id - first tile of the row), which needs no hashing or probing
+// because the bounds kernel already knows the row's exact tile span.
+//   BIN_DS rows (span <= SPAN_T): one warp per row, 4 KB table per warp.
+//   BIN_L  rows: one CTA per row, the span processed in chunks of DCH_COUNT
+//                tiles (64 KB); B tile ranges restricted per chunk by binary
+//                search when the span needs more than one chunk.
+// Every B tile access is a coalesced 4+8 byte load of the flat (A entry,
+// B tile) sequence, 32 lanes busy regardless of row lengths.
+#include "hsmu_block.cuh"
+#include "hsmu_kernels.h"
+
+namespace hsmu {
+
+constexpr int DS_WARPS = 8;
+
+__global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__restrict__ arp,
+                                                            const int *__restrict__ acol,
+                                                            const int *__restrict__ tptr,
+                                                            const int *__restrict__ tcol,
+                                                            const unsigned long long *__restrict__ tmask,
+                                                            RowInfo ri, Ctl *ctl) {
+    __shared__ unsigned long long s_mask[DS_WARPS][SPAN_T];
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    unsigned long long *msk = s_mask[w];
+    const int n = ctl->bin_count[BIN_DS];
+    const int *rows = ri.bins + (size_t)BIN_DS * M;
+    for (int r = blockIdx.x * DS_WARPS + w; r < n; r += gridDim.x * DS_WARPS) {
+        const int i = rows[r];
+        const int t0 = ri.tmin[i];
+        const int span = ri.tmax[i] - t0 + 1;
+        for (int t = lane; t < span; t += WARP) msk[t] = 0ull;
+        __syncwarp();
+        bool bad = false;
+        warp_walk_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, 0, 0, [&](int idx) {
+            const int t = __ldg(tcol + idx) - t0;
+            if (t >= 0 && t < span) atomicOr(msk + t, __ldg(tmask + idx));
+            else bad = true;
+        });
+        if (bad) set_err(&ctl->err, DERR_INTERNAL);
+        __syncwarp();
+        int cnt = 0;
+        for (int t = lane; t < span; t += WARP) cnt += popc64(msk[t]);
+        cnt = warp_sum(cnt);
+        if (lane == 0) ri.cnnz[i] = cnt;
+        __syncwarp();
+    }
+}
+
+constexpr int L_THREADS = 256;
+
+__global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restrict__ arp,
+                                                       const int *__restrict__ acol,
+                                                       const int *__restrict__ tptr,
+                                                       const int *__restrict__ tcol,
+                                                       const unsigned long long *__restrict__ tmask,
+                                                       RowInfo ri, Ctl *ctl) {
+    extern __shared__ unsigned long long s_dyn[];
+    unsigned long long *msk = s_dyn;  // DCH_COUNT entries
+    __shared__ int s_red[L_THREADS / 32];
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    constexpr int NWARP = L_THREADS / 32;
+    const int n = ctl->bin_count[BIN_L];
+    const int *rows = ri.bins + (size_t)BIN_L * M;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const int i = rows[r];
+        const int tmin = ri.tmin[i], tmax = ri.tmax[i];
+        const int a_lo = arp[i], a_hi = arp[i + 1];
+        const bool one_chunk = (tmax - tmin + 1) <= DCH_COUNT;
+        int total = 0;
+        for (int c0 = tmin; c0 <= tmax; c0 += DCH_COUNT) {
+            const int c1 = min(c0 + DCH_COUNT, tmax + 1);
+            for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) msk[t] = 0ull;
+            __syncthreads();
+            bool bad = false;
+            auto orfn = [&](int idx) {
+                const int t = __ldg(tcol + idx) - c0;
+                if (t >= 0 && t < c1 - c0) atomicOr(msk + t, __ldg(tmask + idx));
+                else bad = true;
+            };
+            if (one_chunk)
+                warp_walk_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+            else
+                warp_walk_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+            if (bad) set_err(&ctl->err, DERR_INTERNAL);
+            __syncthreads();
+            int cnt = 0;
+            for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) cnt += popc64(msk[t]);
+            cnt = warp_sum(cnt);
+            if (lane == 0) s_red[w] = cnt;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int s = 0;
+                for (int j = 0; j < NWARP; j++) s += s_red[j];
+                total += s;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) ri.cnnz[i] = total;
+    }
+}
+
+void launch_count(const DevCSR &A, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm, cudaStream_t st) {
+    k_count_ds<<<nsm * 6, DS_WARPS * 32, 0, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, ctl);
+    k_count_l<<<nsm * 3, L_THREADS, DCH_COUNT * sizeof(unsigned long long), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col,
+                                                                                   Bt.mask, ri, ctl);
+}
+
+int configure_count() {
+    return (int)cudaFuncSetAttribute(k_count_l, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     DCH_COUNT * (int)sizeof(unsigned long long));
+}
+
+}  // namespace hsmu

@@ -1,0 +1,294 @@
+"""Python host layer over the C ABI of the GB300 HSMU SpGEMM engine.
+
+This mirrors the reference's operator interface for the C = A*B path
+(``NHC_spgemm(compressed_bin*, NHC_bin*, NHC_CSR *A, NHC_CSR *B, NHC_CSR *C,
+NHC_mask_matrix*)``, src/NHC_spgemm.cuh:7, with the device copies made by
+``HtD_value_col_ptr``, src/loading.cuh:86-94, and the release by
+``free_C_matrix``, src/loading.cuh:151-165): a caller uploads A and B to the
+device, calls :meth:`Engine.spgemm`, and gets a device CSR ``C`` with sorted
+columns and FP64 values, freed when the Python object is released.
+
+PyTorch is used only for device memory and streams.  All compute runs in the
+hand-written sm_103a kernels of ``libhsmu_gb.so``; there is no CPU fallback:
+if the library is missing or no GB300-class device is present, constructing
+an :class:`Engine` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import gen  # noqa: F401  (re-exported: seeded workload generators)
+from .gen import CSR
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libhsmu_gb.so")
+
+HSMU_OK = 0
+STATUS = {0: "HSMU_OK", 1: "HSMU_ERR_INVALID", 2: "HSMU_ERR_ALLOC", 3: "HSMU_ERR_CUDA",
+          4: "HSMU_ERR_OVERFLOW", 5: "HSMU_ERR_UNSORTED", 6: "HSMU_ERR_INTERNAL",
+          7: "HSMU_ERR_TIMEOUT", 8: "HSMU_ERR_NO_DEVICE"}
+
+# every symbol include/hsmu_gb.h declares (checked by the CPU test suite)
+EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_handle_destroy",
+           "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_btiles_build", "hsmu_btiles_free",
+           "hsmu_csr_free", "hsmu_csr_download"]
+
+
+class HsmuError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+class c_csr(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int32), ("N", ctypes.c_int32), ("nnz", ctypes.c_int32),
+                ("owned", ctypes.c_int32), ("row_ptr", ctypes.c_void_p), ("col", ctypes.c_void_p),
+                ("val", ctypes.c_void_p)]
+
+
+class c_btiles(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int32), ("N", ctypes.c_int32), ("ntiles", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("tile_ptr", ctypes.c_void_p),
+                ("tile_col", ctypes.c_void_p), ("mask", ctypes.c_void_p),
+                ("tile_off", ctypes.c_void_p)]
+
+
+class c_opts(ctypes.Structure):
+    _fields_ = [("validate", ctypes.c_int32), ("arith", ctypes.c_int32),
+                ("window_cap", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+
+
+class c_stats(ctypes.Structure):
+    _fields_ = [("products", ctypes.c_uint64), ("nnz_c", ctypes.c_int64),
+                ("ntiles_b", ctypes.c_int64), ("windows", ctypes.c_int64),
+                ("ms_convert", ctypes.c_float), ("ms_symbolic", ctypes.c_float),
+                ("ms_alloc", ctypes.c_float), ("ms_structure", ctypes.c_float),
+                ("ms_numeric", ctypes.c_float), ("ms_total", ctypes.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libhsmu_gb.so (raises OSError if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError("libhsmu_gb.so not built: run __graft_entry__.build() (missing %s)" % path)
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    L.hsmu_strerror.restype = ctypes.c_char_p
+    L.hsmu_strerror.argtypes = [ctypes.c_int]
+    L.hsmu_abi_version.restype = ctypes.c_int
+    L.hsmu_handle_create.argtypes = [ctypes.POINTER(P)]
+    L.hsmu_handle_destroy.argtypes = [P]
+    L.hsmu_spgemm.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
+                              ctypes.POINTER(c_opts), P, ctypes.POINTER(c_stats)]
+    L.hsmu_spgemm_tiled.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
+                                    ctypes.POINTER(c_btiles), ctypes.POINTER(c_csr),
+                                    ctypes.POINTER(c_opts), P, ctypes.POINTER(c_stats)]
+    L.hsmu_btiles_build.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_btiles), P]
+    L.hsmu_btiles_free.argtypes = [ctypes.POINTER(c_btiles)]
+    L.hsmu_csr_free.argtypes = [ctypes.POINTER(c_csr)]
+    L.hsmu_csr_download.argtypes = [ctypes.POINTER(c_csr), P, P, P, P]
+    _lib = L
+    return L
+
+
+def _check(rc: int, what: str):
+    if rc != HSMU_OK:
+        msg = load_library().hsmu_strerror(rc).decode()
+        raise HsmuError(rc, "%s: %s" % (what, msg))
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class DeviceCSR:
+    """A CSR matrix in device memory.
+
+    Inputs keep torch tensors alive (``from_host``); outputs of the engine hold
+    library-owned arrays that are released with ``hsmu_csr_free`` on
+    :meth:`free` or garbage collection."""
+
+    def __init__(self, desc: c_csr, keep=None):
+        self.desc = desc
+        self._keep = keep
+
+    @property
+    def M(self):
+        return self.desc.M
+
+    @property
+    def N(self):
+        return self.desc.N
+
+    @property
+    def nnz(self):
+        return self.desc.nnz
+
+    @staticmethod
+    def from_host(A: CSR, device="cuda", pinned_stream=None) -> "DeviceCSR":
+        torch = _torch()
+        rp = torch.from_numpy(np.ascontiguousarray(A.row_ptr, dtype=np.int32)).to(device)
+        col = torch.from_numpy(np.ascontiguousarray(A.col, dtype=np.int32)).to(device)
+        val = torch.from_numpy(np.ascontiguousarray(A.val, dtype=np.float64)).to(device)
+        return DeviceCSR.from_tensors(A.M, A.N, rp, col, val)
+
+    @staticmethod
+    def from_tensors(M: int, N: int, rp, col, val) -> "DeviceCSR":
+        torch = _torch()
+        assert rp.dtype == torch.int32 and col.dtype == torch.int32 and val.dtype == torch.float64
+        assert rp.is_contiguous() and col.is_contiguous() and val.is_contiguous()
+        d = c_csr(M, N, int(col.numel()), 0, rp.data_ptr(), col.data_ptr() if col.numel() else 0,
+                  val.data_ptr() if val.numel() else 0)
+        return DeviceCSR(d, keep=(rp, col, val))
+
+    def to_host(self, stream=None) -> CSR:
+        L = load_library()
+        rp = np.empty(self.M + 1, dtype=np.int32)
+        col = np.empty(self.nnz, dtype=np.int32)
+        val = np.empty(self.nnz, dtype=np.float64)
+        _check(L.hsmu_csr_download(ctypes.byref(self.desc), rp.ctypes.data, col.ctypes.data,
+                                   val.ctypes.data, _stream_ptr(stream)), "hsmu_csr_download")
+        return CSR(self.M, self.N, rp, col, val)
+
+    def free(self):
+        if self.desc.owned:
+            load_library().hsmu_csr_free(ctypes.byref(self.desc))
+        self._keep = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class BTiles:
+    """B converted once to 64-column bit tiles, reusable across products."""
+
+    def __init__(self, engine: "Engine", B: DeviceCSR, stream=None):
+        self.desc = c_btiles()
+        self.B = B
+        _check(load_library().hsmu_btiles_build(engine.handle, ctypes.byref(B.desc),
+                                                ctypes.byref(self.desc), _stream_ptr(stream)),
+               "hsmu_btiles_build")
+
+    @property
+    def ntiles(self):
+        return self.desc.ntiles
+
+    def arrays(self):
+        """(tile_ptr, tile_col, mask, tile_off) copied to host numpy arrays."""
+        T = self.desc.ntiles
+        out = []
+        for ptr, n, dt in ((self.desc.tile_ptr, self.desc.M + 1, np.int32),
+                           (self.desc.tile_col, T, np.int32), (self.desc.mask, T, np.uint64),
+                           (self.desc.tile_off, T, np.int32)):
+            a = np.empty(n, dtype=dt)
+            if n:
+                _memcpy_d2h(a.ctypes.data, ptr, a.nbytes)
+            out.append(a)
+        return tuple(out)
+
+    def free(self):
+        if self.desc.tile_ptr:
+            load_library().hsmu_btiles_free(ctypes.byref(self.desc))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+_cudart = None
+
+
+def _memcpy_d2h(dst: int, src: int, nbytes: int) -> None:
+    """Synchronous device-to-host copy through the CUDA runtime the engine links."""
+    global _cudart
+    if _cudart is None:
+        load_library()
+        _cudart = ctypes.CDLL("libcudart.so.13")
+        _cudart.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+        _cudart.cudaMemcpy.restype = ctypes.c_int
+    rc = _cudart.cudaMemcpy(dst, src, nbytes, 2)  # cudaMemcpyDeviceToHost
+    if rc != 0:
+        raise HsmuError(3, "cudaMemcpy failed (%d)" % rc)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        torch = _torch()
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return ctypes.c_void_p(stream)
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class Engine:
+    """One library handle on the current CUDA device (hsmu_handle_create)."""
+
+    def __init__(self):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise HsmuError(8, "no CUDA device: the engine has no CPU path")
+        torch.cuda.init()
+        L = load_library()
+        h = ctypes.c_void_p()
+        _check(L.hsmu_handle_create(ctypes.byref(h)), "hsmu_handle_create")
+        self.handle = h
+        self.last_stats: dict | None = None
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load_library().hsmu_handle_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def spgemm(self, A: DeviceCSR, B: DeviceCSR, *, validate: bool = False, arith: int = 0,
+               tiles: BTiles | None = None, stream=None, stats: bool = False) -> DeviceCSR:
+        """C = A * B on the device (hsmu_spgemm / hsmu_spgemm_tiled)."""
+        L = load_library()
+        C = c_csr()
+        o = c_opts(int(validate), int(arith), 0)
+        st = c_stats()
+        sp = ctypes.byref(st) if stats else None
+        if tiles is None:
+            rc = L.hsmu_spgemm(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc), ctypes.byref(C),
+                               ctypes.byref(o), _stream_ptr(stream), sp)
+        else:
+            rc = L.hsmu_spgemm_tiled(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc),
+                                     ctypes.byref(tiles.desc), ctypes.byref(C), ctypes.byref(o),
+                                     _stream_ptr(stream), sp)
+        _check(rc, "hsmu_spgemm")
+        self.last_stats = st.as_dict() if stats else None
+        return DeviceCSR(C)
+
+
+def spgemm_host(A: CSR, B: CSR, engine: Engine | None = None, **kw) -> CSR:
+    """Convenience: upload A and B, multiply on the GPU, download C."""
+    eng = engine or Engine()
+    dA = DeviceCSR.from_host(A)
+    dB = dA if B is A else DeviceCSR.from_host(B)
+    C = eng.spgemm(dA, dB, **kw)
+    out = C.to_host()
+    C.free()
+    return out

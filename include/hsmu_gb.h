@@ -1,0 +1,144 @@
+/*
+ * hsmu_gb.h -- C ABI of the GB300 (sm_103a) HSMU SpGEMM engine, C = A * B.
+ *
+ * CSR in, CSR out: int32 row pointers and column indices, FP64 values,
+ * zero-based, columns strictly increasing within each row.  All matrix
+ * arrays passed to the compute entry points live in device memory of the
+ * current CUDA device.  No torch or CUDA types appear in the signatures:
+ * streams are passed as `void *` (a cudaStream_t, NULL = legacy default).
+ *
+ * Every function returns an hsmu_status (0 = success); no C++ exception
+ * crosses this boundary.  The C++ compatibility layer in hsmu_nhc_compat.h
+ * maps non-zero codes to std::exception as the reference's CHECK_ERROR does.
+ *
+ * Reference interfaces replaced (paths relative to the HSMU-SpGEMM project):
+ *   hsmu_spgemm          <- void NHC_spgemm(compressed_bin*, NHC_bin*, NHC_CSR *A,
+ *                           NHC_CSR *B, NHC_CSR *C, NHC_mask_matrix*)
+ *                           src/NHC_spgemm.cuh:7, whose compressed branch is
+ *                           compressed_NHC_spgemm, src/compressed/compressed_NHC_spgemm.cu:22
+ *   hsmu_handle_create   <- setup(), src/loading.cuh:51-84 (streams, scratch, scan storage)
+ *   hsmu_handle_destroy  <- realse_compressed_bin / free_bin, src/loading.cuh:106-130,166-173
+ *   hsmu_csr_free        <- free_C_matrix, src/loading.cuh:151-165
+ *   hsmu_btiles_build    <- Initialize_compressed_mask64_matrix,
+ *                           src/compressed/compressed_mask64.cuh:343-424
+ *   hsmu_btiles_free     <- realse_NHC_tile, src/loading.cuh:95-105
+ *   hsmu_strerror        <- (none: the reference prints and throws, inc/cuda_comm.h:16-29)
+ */
+#ifndef HSMU_GB_H
+#define HSMU_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HSMU_ABI_VERSION 1
+
+typedef enum hsmu_status {
+    HSMU_OK = 0,
+    HSMU_ERR_INVALID = 1,      /* bad argument, shape mismatch, NULL pointer */
+    HSMU_ERR_ALLOC = 2,        /* device or host allocation failed */
+    HSMU_ERR_CUDA = 3,         /* a CUDA runtime call or kernel launch failed */
+    HSMU_ERR_OVERFLOW = 4,     /* nnz(C) or a scratch size does not fit int32 */
+    HSMU_ERR_UNSORTED = 5,     /* validation: columns not strictly increasing / out of range */
+    HSMU_ERR_INTERNAL = 6,     /* a device-side consistency check failed */
+    HSMU_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up */
+    HSMU_ERR_NO_DEVICE = 8     /* no usable sm_103 device */
+} hsmu_status;
+
+/* CSR matrix descriptor.  row_ptr has M+1 entries, col/val have nnz entries.
+ * `owned` = 1 when the arrays were allocated by this library (output of
+ * hsmu_spgemm); hsmu_csr_free releases exactly those. */
+typedef struct hsmu_csr {
+    int32_t M;
+    int32_t N;
+    int32_t nnz;
+    int32_t owned;
+    int32_t *row_ptr;
+    int32_t *col;
+    double *val;
+} hsmu_csr;
+
+/* B converted to 64-column bit tiles (the reference's compressed mask64
+ * format, one u64 per non-empty 64-column tile of a row):
+ *   tile_ptr[M+1]  tiles of row k are tile_ptr[k] .. tile_ptr[k+1]-1
+ *   tile_col[T]    tile index (column >> 6), strictly increasing per row
+ *   mask[T]        bit b set  <=> column tile_col*64 + b is present
+ *   tile_off[T]    CSR offset of the tile's first entry in B
+ * The same tiles may be reused for every product with the same B. */
+typedef struct hsmu_btiles {
+    int32_t M;
+    int32_t N;
+    int32_t ntiles;
+    int32_t reserved;
+    int32_t *tile_ptr;
+    int32_t *tile_col;
+    uint64_t *mask;
+    int32_t *tile_off;
+} hsmu_btiles;
+
+/* Options; a NULL pointer means all defaults (zero-initialise to get them). */
+typedef struct hsmu_opts {
+    int32_t validate;     /* 1: check A and B are canonical CSR before computing */
+    int32_t arith;        /* 0: auto (integer-pipe exact multiply mixed with FP64 pipe), 1: FP64 pipe only */
+    int32_t window_cap;   /* 0: default slots per numeric window (<= 4096) */
+    int32_t reserved[5];
+} hsmu_opts;
+
+/* Per-call statistics (filled by hsmu_spgemm when stats != NULL). */
+typedef struct hsmu_stats {
+    uint64_t products;       /* intermediate products sum nnz(B(k,:)) over A entries */
+    int64_t nnz_c;
+    int64_t ntiles_b;
+    int64_t windows;         /* numeric work items */
+    float ms_convert;        /* B -> tiles */
+    float ms_symbolic;       /* bounds, binning, exact count, scan */
+    float ms_alloc;          /* output allocation (includes the one host read of nnz) */
+    float ms_structure;      /* column emission */
+    float ms_numeric;        /* value accumulation */
+    float ms_total;
+} hsmu_stats;
+
+typedef struct hsmu_handle_s *hsmu_handle;
+
+const char *hsmu_strerror(int status);
+int hsmu_abi_version(void);
+
+/* Library context for the current device: scratch pool, events, cached
+ * device properties.  One handle per host thread (not reentrant). */
+int hsmu_handle_create(hsmu_handle *out);
+int hsmu_handle_destroy(hsmu_handle h);
+
+/* C = A * B.  A, B: device CSR (A->N == B->M).  On success C->M = A->M,
+ * C->N = B->N, C->nnz is set and C->row_ptr/col/val are new device arrays
+ * owned by the library (free with hsmu_csr_free).  Columns of every C row
+ * are sorted ascending; entries whose products cancel to 0.0 are kept.
+ * Values: each product a_ik*b_kj is rounded to double, then added to the
+ * entry in the order of A(i,:)'s storage (bit-identical run to run).
+ * Stream-ordered on `stream`; returns after one host read of nnz(C) and
+ * leaves the remaining kernels queued on `stream`. */
+int hsmu_spgemm(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C,
+                const hsmu_opts *opts, void *stream, hsmu_stats *stats);
+
+/* Same, with B already converted by hsmu_btiles_build (B tiles reused). */
+int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B,
+                      const hsmu_btiles *Bt, hsmu_csr *C, const hsmu_opts *opts,
+                      void *stream, hsmu_stats *stats);
+
+int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream);
+int hsmu_btiles_free(hsmu_btiles *t);
+
+/* Releases the arrays of a library-owned CSR (owned == 1) and zeroes it. */
+int hsmu_csr_free(hsmu_csr *C);
+
+/* Copies a device CSR into caller-provided host buffers (pinned or pageable):
+ * row_ptr[M+1], col[nnz], val[nnz].  Stream-ordered; synchronizes `stream`
+ * before returning. */
+int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HSMU_GB_H */
