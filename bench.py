@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 HSMU SpGEMM engine, C = A*B (int32 CSR, FP64).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+                    [--workload NAME]
+
+One step = one C = A*B through the engine's C ABI (hsmu_spgemm: B tile
+conversion, bounds, exact symbolic count, scan, output allocation, sorted
+structure, values) with A and B already resident in HBM; the step's output
+is freed after it.  `value` is 2 * intermediate products / step time
+(GFLOPS, the reference's own definition, src/compressed/compressed_NHC_spgemm.cu:191-202),
+summed over ranks.  `e2e` is the same metric through the same public call
+with host buffers: pinned host -> device copy of A and B, the product, and
+device -> pinned host copy of C inside the timed region.
+
+Default workload: the FEM-like 27-point stencil on a 40^3 grid with 3 dofs
+per node (n = 192,000, nnz = 14.8M), C = A*A, values uniform(-1,1), seed 1.
+Inputs (A, B = 177 MB each) and the output (789 MB) are larger than L2.
+
+`--impl reference` times the CPU arm on the host cores: the host FP64
+Gustavson restatement of the reference's path (the reference itself has no
+CPU implementation of C = A*B), with every host thread, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "hsmu-spgemm_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "SpGEMM GFLOPS + HBM GB/s, 1 GB300, plain vs learned/batched, ≤1e-12 rel FP64"
+FALLBACK_HBM_GBS = 6800.0
+# FP64 pipe: DADD/DMUL/DFMA lane-ops per second on GB300 (152 SMs), measured
+# with a dependent-chain throughput probe: 1.61 lane-ops/clk/SM at 2070 MHz.
+FP64_LANE_OPS_PER_S = 5.06e11
+
+WORKLOADS = {
+    "stencil27_40_dof3_AA": "27-point stencil, 40^3 grid x 3 dofs (n=192,000), C=A*A, uniform(-1,1), seed 1",
+    "laplacian2d_256_AA": "5-point Laplacian, 256^2 grid (n=65,536), C=A*A, uniform(-1,1), seed 0",
+    "rmat18_AA": "R-MAT scale 18, edge factor 16, (0.57,0.19,0.19,0.05), merged, uniform(0,1), seed 2, C=A*A",
+    "rmat18_AAt": "R-MAT scale 18, edge factor 16, merged, uniform(0,1), seed 2, C=A*A^T",
+}
+
+
+def make_workload(name):
+    from hsmu_gb import gen
+
+    if name == "stencil27_40_dof3_AA":
+        A = gen.stencil27(40, 3, seed=1)
+        return A, A
+    if name == "laplacian2d_256_AA":
+        A = gen.laplacian2d(256, seed=0)
+        return A, A
+    if name == "rmat18_AA":
+        A = gen.rmat(18, 16, seed=2)
+        return A, A
+    if name == "rmat18_AAt":
+        A = gen.rmat(18, 16, seed=2)
+        return A, gen.transpose(A)
+    raise SystemExit("unknown workload %s" % name)
+
+
+def csr_bytes(M, nnz):
+    return 4 * (M + 1) + 12 * nnz
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup(n_gpus):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def cpu_oracle_run(A, B, max_products=1.2e9, reps=3):
+    """Time the host Gustavson oracle (all host threads) on A*B or a row sample."""
+    import numpy as np
+
+    import oracle
+    from hsmu_gb import gen
+
+    total = gen.products(A, B)
+    rows = None
+    sample = "all %d rows" % A.M
+    prods = total
+    if total > max_products:
+        step = int(np.ceil(total / max_products))
+        rows = np.arange(0, A.M, step, dtype=np.int32)
+        blen = np.diff(B.row_ptr).astype(np.int64)
+        prods = int(sum(int(blen[A.col[A.row_ptr[r]:A.row_ptr[r + 1]]].sum()) for r in rows))
+        sample = "every %d-th row (%d rows, %d products)" % (step, rows.size, prods)
+    nthreads = oracle.max_threads()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.spgemm(A, B, rows=rows, nthreads=nthreads)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return {"value": 2.0 * prods / t / 1e9, "unit": "GFLOPS", "cores": nthreads, "kind": "port",
+            "sample": sample + ", median of %d" % reps, "seconds": t}
+
+
+def run_reference(args):
+    """CPU arm: the oracle port on the host cores, same workload and metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    A, B = make_workload(args.workload)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_oracle_run(A, B, reps=1)
+    vals, secs = [], []
+    info = None
+    for _ in range(args.steps):
+        info = cpu_oracle_run(A, B, reps=1)
+        vals.append(info["value"])
+        secs.append(info["seconds"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "GFLOPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * statistics.median(secs), 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]},
+            "cpu_baseline": {"value": round(v, 3), "unit": "GFLOPS", "cores": info["cores"],
+                             "kind": "port", "sample": info["sample"]},
+            "e2e": {"value": round(v, 3), "unit": "GFLOPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import numpy as np
+    import torch
+
+    import hsmu_gb
+    from hsmu_gb import gen
+
+    rank, world, local = dist_setup(args.gpus)
+    A, B = make_workload(args.workload)
+    same = B is A
+    eng = hsmu_gb.Engine()
+    dA = hsmu_gb.DeviceCSR.from_host(A)
+    dB = dA if same else hsmu_gb.DeviceCSR.from_host(B)
+    products = gen.products(A, B)
+    stream = torch.cuda.current_stream()
+
+    # warm-up (also gives nnz(C) for the e2e host buffers)
+    nnz_c = 0
+    for _ in range(args.warmup):
+        C = eng.spgemm(dA, dB, stats=True)
+        nnz_c = C.nnz
+        C.free()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stage = {k: 0.0 for k in ("ms_convert", "ms_symbolic", "ms_alloc", "ms_structure", "ms_numeric")}
+    launches = 0
+    for _ in range(args.steps):
+        C = eng.spgemm(dA, dB, stats=True)
+        st = eng.last_stats
+        for k in stage:
+            stage[k] += st[k]
+        launches += st["launches"]
+        C.free()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop()
+    ms = dist_max(ms, world)
+    value = world * 2.0 * products / (ms * 1e-3) / 1e9
+
+    # ---- end to end through the public API with host buffers
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    hA = (pin(A.row_ptr), pin(A.col), pin(A.val))
+    hB = hA if same else (pin(B.row_ptr), pin(B.col), pin(B.val))
+    gA = tuple(torch.empty_like(x, device="cuda") for x in hA)
+    gB = gA if same else tuple(torch.empty_like(x, device="cuda") for x in hB)
+    oC = (torch.empty(A.M + 1, dtype=torch.int32).pin_memory(),
+          torch.empty(nnz_c, dtype=torch.int32).pin_memory(),
+          torch.empty(nnz_c, dtype=torch.float64).pin_memory())
+    h2d = sum(x.numel() * x.element_size() for x in hA) + (0 if same else sum(
+        x.numel() * x.element_size() for x in hB))
+    d2h = sum(x.numel() * x.element_size() for x in oC)
+    L = hsmu_gb.load_library()
+
+    def e2e_step():
+        for g, h in zip(gA, hA):
+            g.copy_(h, non_blocking=True)
+        if not same:
+            for g, h in zip(gB, hB):
+                g.copy_(h, non_blocking=True)
+        dA2 = hsmu_gb.DeviceCSR.from_tensors(A.M, A.N, *gA)
+        dB2 = dA2 if same else hsmu_gb.DeviceCSR.from_tensors(B.M, B.N, *gB)
+        C = eng.spgemm(dA2, dB2)
+        import ctypes
+
+        rc = L.hsmu_csr_download(ctypes.byref(C.desc), oC[0].data_ptr(), oC[1].data_ptr(),
+                                 oC[2].data_ptr(), ctypes.c_void_p(stream.cuda_stream))
+        if rc:
+            raise RuntimeError("download failed %d" % rc)
+        C.free()
+
+    e2e_step()
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ke = max(1, min(args.steps, 5))
+    for _ in range(ke):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = dist_max(e0.elapsed_time(e1) / ke, world)
+    e2e_value = world * 2.0 * products / (e2e_ms * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel (numeric: reads A, B and C's columns, writes C's values)
+    peak, peak_kind = load_peaks()
+    alg_bytes = csr_bytes(A.M, A.nnz) + csr_bytes(B.M, B.nnz) + csr_bytes(A.M, nnz_c)
+    num_ms = stage["ms_numeric"] / args.steps
+    achieved = alg_bytes / (num_ms * 1e-3) / 1e9
+    fp64_ach = 2.0 * products / (num_ms * 1e-3)  # FP64 lane-ops/s (one DMUL + one DADD per product)
+
+    if rank != 0:
+        return
+    cpu = cpu_oracle_run(A, B)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GFLOPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator; the reference's SuiteSparse inputs are not available)",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload], "n": A.M,
+                   "nnz_A": A.nnz, "nnz_B": B.nnz, "nnz_C": nnz_c, "products": products,
+                   "l2": "inputs and output larger than L2 (A %.0f MB, C %.0f MB > 129 MB)" % (
+                       csr_bytes(A.M, A.nnz) / 1e6, csr_bytes(A.M, nnz_c) / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "hbm_gbs_step": round(alg_bytes / (ms * 1e-3) / 1e9, 2),
+        "stages_ms": {k: round(v / args.steps, 4) for k, v in stage.items()},
+        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": round(achieved, 2),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "traffic": None,
+                     "alg_bytes": alg_bytes, "ms": round(num_ms, 4)},
+        "fp64_pipe": {"achieved_lane_ops_per_s": fp64_ach, "peak_lane_ops_per_s": FP64_LANE_OPS_PER_S,
+                      "frac": round(fp64_ach / FP64_LANE_OPS_PER_S, 4),
+                      "note": "numeric kernel: one DMUL + one DADD per product"},
+        "cpu_baseline": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in cpu.items()
+                         if k != "seconds"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "GFLOPS", "ms_per_step": round(e2e_ms, 4),
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--workload", default="stencil27_40_dof3_AA", choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

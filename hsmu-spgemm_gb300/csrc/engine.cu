@@ -223,7 +223,7 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
     if (stats) cudaEventRecord(h->ev[3], st);
 
     // 5a. structure + windows
-    if (hc.nnz > 0) launch_structure(Ad, Btd, ri, crp, ccol, win, win_cap, ctl, h->nsm, st);
+    if (hc.nnz > 0) launch_structure(Ad, Bd, Btd, ri, crp, ccol, cval, win, win_cap, ctl, o.arith, h->nsm, st);
     if (stats) cudaEventRecord(h->ev[4], st);
     // 5b. values
     if (hc.nnz > 0) launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, ctl, o.arith, h->nsm, st);
@@ -266,6 +266,8 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
         stats->ms_numeric = t;
         cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
         stats->ms_total = t;
+        // validate 2, tiles 5 (count, 3 scan, fill), bounds 1, count 2, scan 3, structure 2, numeric 1
+        stats->launches = (o.validate ? 2 : 0) + (Bt_in ? 0 : 5) + 6 + (hc.nnz > 0 ? 3 : 0);
     }
 done:
     pfree(ctl, st);
@@ -406,6 +408,14 @@ int hsmu_csr_free(hsmu_csr *C) {
     }
     std::memset(C, 0, sizeof(*C));
     return HSMU_OK;
+}
+
+int hsmu_selftest_dmul(uint64_t n, uint64_t seed, uint64_t *mismatches, void *stream) {
+    if (!mismatches) return HSMU_ERR_INVALID;
+    unsigned long long m = 0;
+    int e = run_dmul_selftest(n, seed, &m, static_cast<cudaStream_t>(stream));
+    *mismatches = m;
+    return e ? HSMU_ERR_CUDA : HSMU_OK;
 }
 
 int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream) {

@@ -21,17 +21,19 @@ __device__ __forceinline__ int seg_of(int incl, int g) {
 
 // Visit every B tile of the rows referenced by A entries [a_lo, a_hi), with
 // the tile range of each B row optionally restricted to tile ids [c0, c1)
-// (restrict = true: lower_bound on the sorted tile ids).  Lanes take 32
-// consecutive flat items at a time, so every lane is busy regardless of the
-// B row lengths.  fn(tile_index) is called for valid items only.  The walk
-// starts at A entry a_lo + first and advances `stride` entries per step
-// (first/stride let several warps of a CTA share one row).
+// (RESTRICT: lower_bound on the sorted tile ids).  The A entries are taken
+// 32 at a time (one per lane: segment = that entry's B tile range); the flat
+// sequence of (A entry, B tile) items is then shared out in steps of 32
+// consecutive items, starting at flat offset `first` and advancing `stride`
+// items, so one warp (first 0, stride 32) or all warps of a CTA
+// (first 32*w, stride 32*nwarps) keep every lane busy whatever the B row
+// lengths.  fn(tile_index) is called for valid items only.
 template <bool RESTRICT, class Fn>
 __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, int stride,
                                                 const int *__restrict__ acol, const int *__restrict__ tptr,
                                                 const int *__restrict__ tcol, int c0, int c1, Fn fn) {
     const int lane = lane_id();
-    for (int pb = a_lo + first; pb < a_hi; pb += stride) {
+    for (int pb = a_lo; pb < a_hi; pb += WARP) {
         const int p = pb + lane;
         int lo = 0, hi = 0;
         if (p < a_hi) {
@@ -47,7 +49,7 @@ __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, i
         const int incl = warp_incl_scan(len);
         const int total = __shfl_sync(FULL, incl, WARP - 1);
         const int excl = incl - len;
-        for (int f = 0; f < total; f += WARP) {
+        for (int f = first; f < total; f += stride) {
             const int g = f + lane;
             const int s = seg_of(incl, g);
             const int idx = __shfl_sync(FULL, lo, s) + (g - __shfl_sync(FULL, excl, s));

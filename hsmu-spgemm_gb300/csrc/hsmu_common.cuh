@@ -17,14 +17,20 @@ namespace hsmu {
 constexpr int WARP = 32;
 constexpr unsigned FULL = 0xffffffffu;
 
-// A C row (or numeric window) whose tile span is at most SPAN_T tiles is
-// handled by one warp with a dense per-tile table in shared memory.
+// A C row whose tile span is at most SPAN_T tiles is handled by one warp
+// with a dense per-tile table in shared memory (symbolic / structure).
 constexpr int SPAN_T = 512;
-// Maximum slots (C entries) of one numeric window; windows are cut at tile
-// boundaries whose slot base crosses a multiple of WIN_CUT, so a window holds
-// at most WIN_CUT + 63 < WIN_CAP slots.
+// Numeric windows: consecutive tiles of one C row with
+//   < WIN_CAP slots (cut where the tile's first slot crosses a multiple of WIN_CUT),
+//   <= WIN_TCAP tiles (cut where the tile's rank in the row crosses a multiple of WIN_TCAP),
+//   a tile span of <= WIN_SPAN tiles (cut at multiples of WIN_SPAN from the row's first tile),
+// so that the numeric kernel's two-level tile table (occupancy bitmap of
+// WIN_SPAN bits + WIN_TCAP rank-ordered masks) and accumulator fit one warp.
 constexpr int WIN_CAP = 1024;
 constexpr int WIN_CUT = WIN_CAP - 64;
+constexpr int WIN_TCAP = 512;
+constexpr int WIN_SPAN = 4096;
+constexpr int WIN_OCCW = WIN_SPAN / 64;
 // Tiles per chunk of the CTA (large-row) kernels.
 constexpr int DCH_COUNT = 8192;   // count pass: 8 B per tile  -> 64 KB
 constexpr int DCH_STRUCT = 8192;  // structure pass: 12 B per tile -> 96 KB
@@ -103,6 +109,19 @@ __device__ __forceinline__ int lower_bound_i32(const int *__restrict__ a, int lo
         if (__ldg(a + mid) < key) lo = mid + 1; else hi = mid;
     }
     return lo;
+}
+
+// first index in [lo, hi) with a[idx] > key, searching forward from lo by
+// doubling steps (cheap when the answer is close to lo)
+__device__ __forceinline__ int gallop_gt(const int *__restrict__ a, int lo, int hi, int key) {
+    if (lo >= hi || __ldg(a + lo) > key) return lo;
+    int prev = lo, step = 1;
+    while (prev + step < hi && __ldg(a + prev + step) <= key) {
+        prev += step;
+        step <<= 1;
+    }
+    const int l = prev + 1, h = min(prev + step, hi);
+    return lower_bound_i32(a, l, h, key + 1);
 }
 
 __device__ __forceinline__ void set_err(int *err, int bit) { atomicOr(err, bit); }

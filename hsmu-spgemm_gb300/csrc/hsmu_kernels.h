@@ -51,12 +51,15 @@ void launch_scan(const int *in, int *out, int n, long long *total64, int *tmp, C
 void launch_count(const DevCSR &A, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm, cudaStream_t st);
 
 // k_structure.cu
-void launch_structure(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol, Window *win,
-                      long long win_cap, Ctl *ctl, int nsm, cudaStream_t st);
+// writes C's columns and numeric windows; rows that fit one warp also get their values
+void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol,
+                      double *cval, Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
 
 // k_numeric.cu
 void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, const int *ccol, double *cval,
                     const Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
+
+int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st);
 
 // smem sizes are set once per device (cudaFuncSetAttribute)
 int configure_kernels();

@@ -1,0 +1,166 @@
+// The product loop shared by the fused row kernel (k_struct_ds) and the
+// window kernel (k_numeric): accumulate a_ik * b_kj into a shared-memory
+// accumulator for one C row (or one window of it), in the oracle's order.
+//
+// Order: for each C entry the products are added as 0.0 + p_1 + p_2 + ...
+// in A(i,:)'s storage order; each p = a*b is rounded first (no FMA), exactly
+// like the host Gustavson oracle, so results are bit-identical to it.
+//
+// The A entries are taken 32 at a time (one per lane); seg(p) gives the B
+// entry range [elo, ehi) that A entry p contributes to this accumulator.
+//   * long B segments (average >= 32 entries): one segment at a time, 32
+//     entries per step.  Entries of one B row have distinct columns, so a
+//     step has no slot conflicts and only a change of segment needs a warp
+//     sync.  The next step's B loads are issued before the current step's
+//     multiply/lookup/add (one-deep software pipeline).
+//   * short B segments: the flat sequence of (A entry, B entry) items, 32 per
+//     step; lanes that hit the same slot in one step (__match_any_sync) add in
+//     lane order = A-entry order.
+#pragma once
+#include "hsmu_block.cuh"
+#include "hsmu_dmul.cuh"
+
+namespace hsmu {
+
+template <bool INT_MUL>
+__device__ __forceinline__ double prod_mul(double a, double b) {
+    if (INT_MUL) return dmul_int(a, b);
+    return __dmul_rn(a, b);
+}
+
+// SegFn:    void(int p, int k, int &elo, int &ehi)  -- called for valid lanes
+// LookupFn: int(int j) -> slot in acc, or -1 if j is not in the accumulator
+template <bool INT_MUL, class SegFn, class LookupFn>
+__device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *__restrict__ acol,
+                                                const double *__restrict__ aval, const int *__restrict__ brp,
+                                                const int *__restrict__ bcol, const double *__restrict__ bval,
+                                                SegFn seg, LookupFn lookup, double *acc, bool &bad) {
+    const int lane = lane_id();
+    for (int pb = a_lo; pb < a_hi; pb += WARP) {
+        const int p = pb + lane;
+        int elo = 0, ehi = 0;
+        double a = 0.0;
+        if (p < a_hi) {
+            const int k = __ldg(acol + p);
+            a = __ldg(aval + p);
+            seg(p, k, elo, ehi);
+        }
+        const int len = ehi - elo;
+        const int incl = warp_incl_scan(len);
+        const int total = __shfl_sync(FULL, incl, WARP - 1);
+        if (total == 0) continue;
+        unsigned todo = __ballot_sync(FULL, len > 0);
+        if (total >= WARP * __popc(todo)) {
+            // ---- long segments: segment-aligned steps of 32, one-deep prefetch
+            int sgi = __ffs(todo) - 1;
+            todo &= todo - 1;
+            int es = __shfl_sync(FULL, elo, sgi), ls = __shfl_sync(FULL, len, sgi);
+            double as = __shfl_sync(FULL, a, sgi);
+            int off = 0;
+            int j0 = 0;
+            double b0 = 0.0;
+            if (lane < ls) {
+                j0 = __ldg(bcol + es + lane);
+                b0 = __ldg(bval + es + lane);
+            }
+            while (true) {
+                int n_off = off + WARP, n_es = es, n_ls = ls;
+                double n_as = as;
+                bool have_next = true, seg_change = false;
+                if (n_off >= ls) {
+                    if (!todo) {
+                        have_next = false;
+                    } else {
+                        const int n_sgi = __ffs(todo) - 1;
+                        todo &= todo - 1;
+                        n_es = __shfl_sync(FULL, elo, n_sgi);
+                        n_ls = __shfl_sync(FULL, len, n_sgi);
+                        n_as = __shfl_sync(FULL, a, n_sgi);
+                        n_off = 0;
+                        seg_change = true;
+                    }
+                }
+                int j1 = 0;
+                double b1 = 0.0;
+                if (have_next && n_off + lane < n_ls) {
+                    j1 = __ldg(bcol + n_es + n_off + lane);
+                    b1 = __ldg(bval + n_es + n_off + lane);
+                }
+                if (off + lane < ls) {
+                    const double pr = prod_mul<INT_MUL>(as, b0);
+                    const int q = lookup(j0);
+                    if (q >= 0) acc[q] = __dadd_rn(acc[q], pr);
+                    else bad = true;
+                }
+                if (!have_next) break;
+                if (seg_change) __syncwarp();
+                es = n_es;
+                ls = n_ls;
+                as = n_as;
+                off = n_off;
+                j0 = j1;
+                b0 = b1;
+            }
+            __syncwarp();
+            continue;
+        }
+        // ---- short segments: flat (A entry, B entry) order, 32 items per step
+        const int excl = incl - len;
+        int sg = seg_of(incl, lane);
+        int j = 0;
+        double b = 0.0, as = __shfl_sync(FULL, a, sg);
+        {
+            const int e = __shfl_sync(FULL, elo, sg) + (lane - __shfl_sync(FULL, excl, sg));
+            if (lane < total) {
+                j = __ldg(bcol + e);
+                b = __ldg(bval + e);
+            }
+        }
+        for (int f = 0; f < total; f += WARP) {
+            const bool gv = f + lane < total;
+            int sg_n = 0, j_n = 0;
+            double b_n = 0.0, as_n = 0.0;
+            if (f + WARP < total) {
+                const int gn = f + WARP + lane;
+                sg_n = seg_of(incl, gn);
+                const int e = __shfl_sync(FULL, elo, sg_n) + (gn - __shfl_sync(FULL, excl, sg_n));
+                as_n = __shfl_sync(FULL, a, sg_n);
+                if (gn < total) {
+                    j_n = __ldg(bcol + e);
+                    b_n = __ldg(bval + e);
+                }
+            }
+            int slot = -1 - lane;
+            double pr = 0.0;
+            if (gv) {
+                pr = prod_mul<INT_MUL>(as, b);
+                const int q = lookup(j);
+                if (q >= 0) slot = q;
+                else bad = true;
+            }
+            const bool act = slot >= 0;
+            const int smin = (int)__reduce_min_sync(FULL, act ? (unsigned)sg : 64u);
+            const int smax = (int)__reduce_max_sync(FULL, act ? (unsigned)sg : 0u);
+            if (smin >= smax) {
+                // one A entry in this step: all slots distinct
+                if (act) acc[slot] = __dadd_rn(acc[slot], pr);
+            } else {
+                const unsigned grp = __match_any_sync(FULL, slot);
+                const int rank = __popc(grp & lanemask_lt());
+                const int maxr = (int)__reduce_max_sync(FULL, act ? (unsigned)rank : 0u);
+                for (int rr = 0; rr < maxr; rr++) {
+                    if (act && rank == rr) acc[slot] = __dadd_rn(acc[slot], pr);
+                    __syncwarp();
+                }
+                if (act && rank == maxr) acc[slot] = __dadd_rn(acc[slot], pr);
+            }
+            __syncwarp();
+            sg = sg_n;
+            j = j_n;
+            b = b_n;
+            as = as_n;
+        }
+    }
+}
+
+}  // namespace hsmu

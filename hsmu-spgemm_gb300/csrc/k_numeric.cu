@@ -6,9 +6,18 @@
 // aval*bval) and of the spECK dense accumulator used for rows with more than
 // 4096 nnz (src/external/spECK/dense_acc.cu:2-267).
 //
-// Slot lookup is O(1): the window's columns are turned back into a dense
-// per-tile table (u64 mask + first slot of the tile), so the slot of column
-// j is base[t] + popc(mask[t] & ((1 << (j & 63)) - 1)) with t = (j >> 6) - t0.
+// Work item: a window = consecutive C tiles of one row (< WIN_CAP slots,
+// <= WIN_TCAP tiles, <= WIN_SPAN tile span), cut by the structure pass.
+// Slot lookup is O(1) through a two-level tile table rebuilt from the
+// window's sorted columns: an occupancy bitmap over the window's tile span
+// with per-word prefix counts gives a tile's rank, and the rank indexes the
+// tile's u64 column mask and first slot:
+//   slot(j) = tbase[r] + popc(tmask[r] & ((1 << (j & 63)) - 1)),
+//   r = opre[t >> 6] + popc(occ[t >> 6] & ((1 << (t & 63)) - 1)),  t = (j >> 6) - t0.
+// A warp takes GW consecutive windows; when the next window continues the
+// same row, the per-A-entry cursors into the B rows are carried over in
+// shared memory, so B rows are split at window boundaries by a short forward
+// (galloping) search instead of a fresh binary search per window.
 //
 // Accumulation order is deterministic and equals the oracle's: the products
 // of the window are walked in the flat order (A entry, then B entry), 32 per
@@ -20,21 +29,33 @@
 // atomicAdd).  No floating-point atomics are used.
 //
 // GB300 executes FP64 at ~1.6 lane-ops/clk/SM, two orders of magnitude below
-// its int32 rate, so this kernel is bound by the FP64 pipe, not by HBM.
-#include "hsmu_block.cuh"
+// its int32 rate, so this kernel is bound by the FP64 pipe, not by HBM; the
+// next step's B loads are issued before the current step's lookups and adds.
 #include "hsmu_kernels.h"
+#include "hsmu_products.cuh"
 
 namespace hsmu {
 
-constexpr int NUM_WARPS = 8;
+constexpr int NUM_WARPS = 4;
+constexpr int NUM_CTAS_PER_SM = 3;
+constexpr int KCAP = 512;  // carried cursors (A entries per row)
+constexpr int GW = 8;      // consecutive windows per warp group
 
 struct NumSmem {
-    unsigned long long msk[SPAN_T];
-    int base[SPAN_T];
+    unsigned long long occ[WIN_OCCW];
+    int opre[WIN_OCCW];
+    unsigned long long tmask[WIN_TCAP];
+    int tbase[WIN_TCAP];
     double acc[WIN_CAP];
+    int cur[KCAP];
 };
+static_assert(WIN_OCCW == 2 * WARP, "prefix pass assumes two occupancy words per lane");
 
-__global__ void __launch_bounds__(NUM_WARPS * 32) k_numeric(const int *__restrict__ arp, const int *__restrict__ acol,
+__device__ __forceinline__ unsigned lanemask_le() { return lanemask_lt() | (1u << lane_id()); }
+
+
+template <bool INT_MUL>
+__global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(const int *__restrict__ arp, const int *__restrict__ acol,
                                                             const double *__restrict__ aval,
                                                             const int *__restrict__ brp, const int *__restrict__ bcol,
                                                             const double *__restrict__ bval,
@@ -45,109 +66,185 @@ __global__ void __launch_bounds__(NUM_WARPS * 32) k_numeric(const int *__restric
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
     const int nwin = min(ctl->win_count, win_cap);
+    const int ngroups = (nwin + GW - 1) / GW;
     const int gw = blockIdx.x * NUM_WARPS + w;
     const int nw = gridDim.x * NUM_WARPS;
     bool bad = false;
-    for (int wi = gw; wi < nwin; wi += nw) {
-        const Window W = win[wi];
-        const int row = W.row, s0 = W.s0, cnt = W.cnt, t0 = W.t0;
-        const int c_lo = ccol[s0], c_hi = ccol[s0 + cnt - 1];
-        const int span = (c_hi >> 6) - t0 + 1;
-        if (cnt <= 0 || cnt > WIN_CAP || span <= 0 || span > SPAN_T || (c_lo >> 6) != t0) {
-            bad = true;
-            continue;
-        }
-        const bool full = (s0 == crp[row]) && (cnt == crp[row + 1] - s0);
-        for (int t = lane; t < span; t += WARP) S.msk[t] = 0ull;
-        for (int s = lane; s < cnt; s += WARP) S.acc[s] = 0.0;
-        __syncwarp();
-        for (int s = lane; s < cnt; s += WARP) {
-            const int c = ccol[s0 + s];
-            const int t = (c >> 6) - t0;
-            if (c >= 0 && t >= 0 && t < span) atomicOr(&S.msk[t], 1ull << (c & 63));
-            else bad = true;
-        }
-        __syncwarp();
-        {
-            const int per = (span + WARP - 1) / WARP;
-            const int lo = min(span, lane * per), hi = min(span, lo + per);
-            int sum = 0;
-            for (int t = lo; t < hi; t++) sum += popc64(S.msk[t]);
-            int run = warp_incl_scan(sum) - sum;
-            for (int t = lo; t < hi; t++) {
-                S.base[t] = run;
-                run += popc64(S.msk[t]);
+    for (int g = gw; g < ngroups; g += nw) {
+        int prev_row = -1, prev_end = -1;
+        const int wend = min(nwin, (g + 1) * GW);
+        for (int wi = g * GW; wi < wend; wi++) {
+            const Window W = win[wi];
+            const int row = W.row, s0 = W.s0, cnt = W.cnt, t0 = W.t0;
+            if (cnt <= 0 || cnt > WIN_CAP) {
+                bad = true;
+                prev_row = -1;
+                continue;
             }
-        }
-        __syncwarp();
-        const int a_lo = arp[row], a_hi = arp[row + 1];
-        for (int pb = a_lo; pb < a_hi; pb += WARP) {
-            const int p = pb + lane;
-            int elo = 0, ehi = 0;
-            double a = 0.0;
-            if (p < a_hi) {
-                const int k = __ldg(acol + p);
-                a = __ldg(aval + p);
-                elo = __ldg(brp + k);
-                ehi = __ldg(brp + k + 1);
-                if (!full) {
-                    elo = lower_bound_i32(bcol, elo, ehi, c_lo);
-                    ehi = lower_bound_i32(bcol, elo, ehi, c_hi + 1);
-                }
+            const int c_lo = ccol[s0], c_hi = ccol[s0 + cnt - 1];
+            const int span = (c_hi >> 6) - t0 + 1;
+            if (span <= 0 || span > WIN_SPAN || (c_lo >> 6) != t0) {
+                bad = true;
+                prev_row = -1;
+                continue;
             }
-            const int len = ehi - elo;
-            const int incl = warp_incl_scan(len);
-            const int total = __shfl_sync(FULL, incl, WARP - 1);
-            const int excl = incl - len;
-            for (int f = 0; f < total; f += WARP) {
-                const int g = f + lane;
-                const bool gv = g < total;
-                const int sg = seg_of(incl, g);
-                const int e = __shfl_sync(FULL, elo, sg) + (g - __shfl_sync(FULL, excl, sg));
-                const double as = __shfl_sync(FULL, a, sg);
-                int slot = -1 - lane;
-                double prod = 0.0;
-                if (gv) {
-                    const int j = __ldg(bcol + e);
-                    const double b = __ldg(bval + e);
-                    prod = __dmul_rn(as, b);
-                    const int tt = (j >> 6) - t0;
-                    if (tt >= 0 && tt < span) {
-                        const unsigned long long m = S.msk[tt];
-                        const int bit = j & 63;
-                        if ((m >> bit) & 1ull) slot = S.base[tt] + rank64(m, bit);
-                        else bad = true;
-                    } else {
-                        bad = true;
+            const int row_lo = crp[row], row_hi = crp[row + 1];
+            const int a_lo = arp[row], a_hi = arp[row + 1];
+            const bool first = s0 == row_lo;
+            const bool last = s0 + cnt == row_hi;
+            const bool keep = (a_hi - a_lo) <= KCAP;
+            const bool carry = keep && prev_row == row && prev_end == s0;
+            prev_row = row;
+            prev_end = s0 + cnt;
+
+            // ---- tile table from the window's sorted columns.  dense: span <= WIN_TCAP,
+            // tmask/tbase indexed by tile - t0; otherwise two-level (occupancy + rank).
+            const bool dense = span <= WIN_TCAP;
+            const int nwords = (span + 63) >> 6;
+            if (!dense)
+                for (int q = lane; q < nwords; q += WARP) S.occ[q] = 0ull;
+            for (int q = lane; q < (dense ? span : min(cnt, WIN_TCAP)); q += WARP) S.tmask[q] = 0ull;
+            for (int q = lane; q < cnt; q += WARP) S.acc[q] = 0.0;
+            __syncwarp();
+            {
+                int run = 0, prev_t = -1;
+                for (int sb = 0; sb < cnt; sb += WARP) {
+                    const int s = sb + lane;
+                    const bool v = s < cnt;
+                    const int c = v ? ccol[s0 + s] : 0;
+                    const int t = (c >> 6) - t0;
+                    int tp = __shfl_up_sync(FULL, t, 1);
+                    if (lane == 0) tp = prev_t;
+                    const bool head = v && t != tp;
+                    const unsigned heads = __ballot_sync(FULL, head);
+                    const int rank = dense ? t : run + __popc(heads & lanemask_le()) - 1;
+                    if (v) {
+                        if (t < 0 || t >= span || rank < 0 || rank >= WIN_TCAP) {
+                            bad = true;
+                        } else {
+                            if (head) {
+                                S.tbase[rank] = s;
+                                if (!dense) atomicOr(&S.occ[t >> 6], 1ull << (t & 63));
+                            }
+                            atomicOr(&S.tmask[rank], 1ull << (c & 63));
+                        }
                     }
-                }
-                const bool act = slot >= 0;
-                const unsigned grp = __match_any_sync(FULL, slot);
-                const int rank = __popc(grp & lanemask_lt());
-                const int maxr = (int)__reduce_max_sync(FULL, act ? (unsigned)rank : 0u);
-                for (int rr = 0; rr <= maxr; rr++) {
-                    if (act && rank == rr) S.acc[slot] = __dadd_rn(S.acc[slot], prod);
-                    __syncwarp();
+                    run += __popc(heads);
+                    prev_t = __shfl_sync(FULL, t, min(WARP, cnt - sb) - 1);
                 }
             }
+            __syncwarp();
+            if (!dense) {
+                const int q0 = 2 * lane;
+                const unsigned long long o0 = q0 < nwords ? S.occ[q0] : 0ull;
+                const unsigned long long o1 = q0 + 1 < nwords ? S.occ[q0 + 1] : 0ull;
+                const int c0 = popc64(o0);
+                const int sum = c0 + popc64(o1);
+                const int ex = warp_incl_scan(sum) - sum;
+                if (q0 < nwords) S.opre[q0] = ex;
+                if (q0 + 1 < nwords) S.opre[q0 + 1] = ex + c0;
+            }
+            __syncwarp();
+            // slot of column j, or -1 when j is not in the window (corrupt input)
+            auto lookup = [&](int j) -> int {
+                const int t = (j >> 6) - t0;
+                if ((unsigned)t >= (unsigned)span) return -1;
+                int r = t;
+                if (!dense) {
+                    const unsigned long long ow = S.occ[t >> 6];
+                    if (!((ow >> (t & 63)) & 1ull)) return -1;
+                    r = S.opre[t >> 6] + rank64(ow, t & 63);
+                }
+                const unsigned long long m = S.tmask[r];
+                const int bit = j & 63;
+                if (!((m >> bit) & 1ull)) return -1;
+                return S.tbase[r] + rank64(m, bit);
+            };
+
+            // ---- products in (A entry, B entry) order
+            auto seg = [&](int p, int k, int &elo, int &ehi) {
+                const int bs = __ldg(brp + k), be = __ldg(brp + k + 1);
+                if (carry) elo = S.cur[p - a_lo];
+                else if (first) elo = bs;
+                else elo = lower_bound_i32(bcol, bs, be, c_lo);
+                ehi = last ? be : gallop_gt(bcol, elo, be, c_hi);
+                if (keep) S.cur[p - a_lo] = ehi;
+            };
+            warp_accumulate<INT_MUL>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
+            __syncwarp();
+            for (int q = lane; q < cnt; q += WARP) cval[s0 + q] = S.acc[q];
+            __syncwarp();
         }
-        __syncwarp();
-        for (int s = lane; s < cnt; s += WARP) cval[s0 + s] = S.acc[s];
-        __syncwarp();
     }
     if (__any_sync(FULL, bad) && lane == 0) set_err(&ctl->err, DERR_INTERNAL);
 }
 
 void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, const int *ccol, double *cval,
                     const Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
-    (void)arith;
-    k_numeric<<<nsm * 2, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(A.rp, A.col, A.val, B.rp, B.col, B.val,
-                                                                            crp, ccol, cval, win, (int)win_cap, ctl);
+    auto k = arith == 2 ? k_numeric<true> : k_numeric<false>;
+    k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
+        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, ctl);
 }
 
 int configure_numeric() {
-    return (int)cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    int e = (int)cudaFuncSetAttribute(k_numeric<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      NUM_WARPS * (int)sizeof(NumSmem));
+    if (e) return e;
+    return (int)cudaFuncSetAttribute(k_numeric<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      NUM_WARPS * (int)sizeof(NumSmem));
+}
+
+// self-test of the integer-pipe multiply against the FP64 pipe on n operand
+// pairs drawn from a xorshift stream (all bit patterns, values in (-1,1),
+// short significands); counts mismatching results.
+__global__ void k_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *mism) {
+    unsigned long long bad = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        unsigned long long s = seed ^ (i * 0x9E3779B97F4A7C15ull);
+        auto rnd = [&]() {
+            s ^= s << 13;
+            s ^= s >> 7;
+            s ^= s << 17;
+            return s;
+        };
+        rnd();
+        double a, b;
+        switch (i % 3) {
+        case 0:
+            a = bitsd(rnd());
+            b = bitsd(rnd());
+            break;
+        case 1:
+            a = (double)(rnd() >> 11) * 0x1p-52 - 1.0;
+            b = (double)(rnd() >> 11) * 0x1p-52 - 1.0;
+            break;
+        default: {
+            const int bits = 24 + (int)(rnd() % 8);
+            a = scalbn((double)((rnd() >> (64 - bits)) | (1ull << (bits - 1))), (int)(rnd() % 200) - 100);
+            b = scalbn((double)((rnd() >> (64 - bits)) | (1ull << (bits - 1))), (int)(rnd() % 200) - 100);
+            break;
+        }
+        }
+        const double x = dmul_int(a, b), y = __dmul_rn(a, b);
+        const bool nan2 = (x != x) && (y != y);
+        if (!nan2 && dbits(x) != dbits(y)) bad++;
+    }
+    if (bad) atomicAdd(mism, bad);
+}
+
+int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st) {
+    unsigned long long *d = nullptr;
+    cudaError_t e = cudaMallocAsync(&d, sizeof(unsigned long long), st);
+    if (e) return (int)e;
+    cudaMemsetAsync(d, 0, sizeof(unsigned long long), st);
+    k_dmul_selftest<<<1024, 256, 0, st>>>(n, seed, d);
+    e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(out, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    cudaFreeAsync(d, st);
+    cudaStreamSynchronize(st);
+    return (int)e;
 }
 
 }  // namespace hsmu

@@ -67,7 +67,9 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                 lpos = atomicAdd(&s_cnt[bin], 1);
                 my_prod += (unsigned long long)prod;
                 const long long cap = prod < (long long)N ? prod : (long long)N;
-                my_wb += (unsigned long long)(cap / WIN_CUT + (span - 1) / SPAN_T + 1);
+                // windows per row <= slot cuts + tile-rank cuts + span cuts + 1
+                const long long tl = cap < (long long)span ? cap : (long long)span;
+                my_wb += (unsigned long long)(cap / WIN_CUT + tl / WIN_TCAP + (span - 1) / WIN_SPAN + 1);
             }
         }
         __syncthreads();

@@ -15,29 +15,40 @@
 // rows are split across many warps and SMs (the reference sends rows with
 // more than 4096 nnz to one CTA of the spECK dense accumulator,
 // src/compressed/compressed_Cval.cuh:300-365).
+//
+// Rows of the warp class (tile span <= SPAN_T) with at most FUSE_CAP entries
+// -- every row of the stencil and Laplacian workloads -- are finished in the
+// same warp: the dense tile table that produced the columns is exactly the
+// slot lookup of the value phase (slot = base[t] + popc(mask[t] below j)),
+// so the products are accumulated right away and the values written with no
+// window, no second walk over A and no re-read of C's columns.
 #include "hsmu_block.cuh"
 #include "hsmu_kernels.h"
+#include "hsmu_products.cuh"
 
 namespace hsmu {
 
-constexpr int SDS_WARPS = 8;
-constexpr int SDS_WL = 64;  // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
+constexpr int SDS_WARPS = 4;
+constexpr int SDS_CTAS_PER_SM = 5;
+constexpr int SDS_WL = 64;     // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
+constexpr int FUSE_CAP = 512;  // rows up to this many entries get their values here
 
 struct SdsSmem {
     unsigned long long msk[SPAN_T];
     int base[SPAN_T];
     int wl[SDS_WL];
     int wt[SDS_WL];
+    double acc[FUSE_CAP];
 };
 
-__global__ void __launch_bounds__(SDS_WARPS * 32) k_struct_ds(int M, const int *__restrict__ arp,
-                                                              const int *__restrict__ acol,
-                                                              const int *__restrict__ tptr,
-                                                              const int *__restrict__ tcol,
-                                                              const unsigned long long *__restrict__ tmask,
-                                                              RowInfo ri, const int *__restrict__ crp,
-                                                              int *__restrict__ ccol, Window *__restrict__ win,
-                                                              long long win_cap, Ctl *ctl) {
+template <bool INT_MUL>
+__global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
+    k_struct_ds(int M, const int *__restrict__ arp, const int *__restrict__ acol, const double *__restrict__ aval,
+                const int *__restrict__ brp, const int *__restrict__ bcol, const double *__restrict__ bval,
+                const int *__restrict__ tptr, const int *__restrict__ tcol,
+                const unsigned long long *__restrict__ tmask, RowInfo ri, const int *__restrict__ crp,
+                int *__restrict__ ccol, double *__restrict__ cval, Window *__restrict__ win, long long win_cap,
+                Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     SdsSmem &S = reinterpret_cast<SdsSmem *>(s_dyn)[w];
@@ -83,6 +94,41 @@ __global__ void __launch_bounds__(SDS_WARPS * 32) k_struct_ds(int M, const int *
                 lastkey = run / WIN_CUT;
                 run += popc64(m);
             }
+        }
+        if (nnz <= FUSE_CAP) {
+            // ---- fused values: columns, then products through the same dense table
+            for (int q = lane; q < nnz; q += WARP) S.acc[q] = 0.0;
+            for (int t = lo; t < hi; t++) {
+                unsigned long long m = S.msk[t];
+                if (m) {
+                    int pos = rowbase + S.base[t];
+                    const int cb = (t0 + t) << 6;
+                    while (m) {
+                        ccol[pos++] = cb + (__ffsll((long long)m) - 1);
+                        m &= m - 1ull;
+                    }
+                }
+            }
+            __syncwarp();
+            auto seg = [&](int p, int k, int &elo, int &ehi) {
+                elo = __ldg(brp + k);
+                ehi = __ldg(brp + k + 1);
+            };
+            auto lookup = [&](int j) -> int {
+                const int t = (j >> 6) - t0;
+                if ((unsigned)t >= (unsigned)span) return -1;
+                const unsigned long long m = S.msk[t];
+                const int bit = j & 63;
+                if (!((m >> bit) & 1ull)) return -1;
+                return S.base[t] + rank64(m, bit);
+            };
+            bool vbad = false;
+            warp_accumulate<INT_MUL>(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, seg, lookup, S.acc, vbad);
+            __syncwarp();
+            for (int q = lane; q < nnz; q += WARP) cval[rowbase + q] = S.acc[q];
+            if (__any_sync(FULL, vbad) && lane == 0) set_err(&ctl->err, DERR_INTERNAL);
+            __syncwarp();
+            continue;
         }
         int carry = __shfl_up_sync(FULL, warp_incl_max(lastkey), 1);
         if (lane == 0) carry = -1;
@@ -140,9 +186,16 @@ __global__ void __launch_bounds__(SDS_WARPS * 32) k_struct_ds(int M, const int *
 }
 
 constexpr int SL_THREADS = 256;
-constexpr int SL_WL = 1024;  // > max windows in one chunk (DCH*64/WIN_CUT + DCH/SPAN_T + 1)
+// > max windows in one chunk: DCH*64/WIN_CUT (slot cuts) + DCH/WIN_TCAP (rank cuts) + DCH/WIN_SPAN + 1
+constexpr int SL_WL = 1024;
 constexpr int SL_PER = DCH_STRUCT / SL_THREADS;
-static_assert(DCH_STRUCT % SPAN_T == 0, "chunks must start on span-block boundaries");
+static_assert(DCH_STRUCT % WIN_SPAN == 0, "chunks must start on window span boundaries");
+static_assert(DCH_STRUCT * 64 / WIN_CUT + DCH_STRUCT / WIN_TCAP + DCH_STRUCT / WIN_SPAN + 1 < SL_WL, "window list");
+
+// packed window key of a tile: (first slot / WIN_CUT, rank / WIN_TCAP, chunk-relative tile / WIN_SPAN)
+__device__ __forceinline__ long long win_key(int base, int rank, int t) {
+    return ((long long)(base / WIN_CUT) << 32) | ((long long)(rank / WIN_TCAP) << 8) | (long long)(t / WIN_SPAN);
+}
 
 struct SlSmem {
     unsigned long long msk[DCH_STRUCT];
@@ -161,6 +214,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
     extern __shared__ unsigned long long s_dyn[];
     SlSmem &S = *reinterpret_cast<SlSmem *>(s_dyn);
     __shared__ int s_tmp[SL_THREADS / 32 + 1];
+    __shared__ long long s_ltmp[SL_THREADS / 32 + 1];
     __shared__ int s_wbase;
     constexpr int NWARP = SL_THREADS / 32;
     const int w = threadIdx.x >> 5;
@@ -173,7 +227,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
         const int rowbase = crp[i];
         const int nnz = crp[i + 1] - rowbase;
         const bool one_chunk = (tmax - tmin + 1) <= DCH_STRUCT;
-        int run_row = 0;
+        int run_row = 0, tiles_row = 0;
         for (int c0 = tmin; c0 <= tmax; c0 += DCH_STRUCT) {
             const int c1 = min(c0 + DCH_STRUCT, tmax + 1);
             const int len = c1 - c0;
@@ -192,26 +246,35 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
             const int lo = min(len, (int)threadIdx.x * SL_PER), hi = min(len, lo + SL_PER);
-            int sum = 0;
-            for (int t = lo; t < hi; t++) sum += popc64(S.msk[t]);
-            int chunk_total;
+            int sum = 0, ntl = 0;
+            for (int t = lo; t < hi; t++) {
+                const unsigned long long m = S.msk[t];
+                sum += popc64(m);
+                ntl += m != 0ull;
+            }
+            int chunk_total, chunk_tiles;
             int run = block_excl_sum<SL_THREADS>(sum, s_tmp, chunk_total) + run_row;
-            int lastkey = -1;
+            int rank = block_excl_sum<SL_THREADS>(ntl, s_tmp, chunk_tiles) + tiles_row;
+            // window key: (first slot / WIN_CUT, tile rank / WIN_TCAP, tile / WIN_SPAN),
+            // packed so that it is non-decreasing along the row
+            long long lastkey = -1;
             for (int t = lo; t < hi; t++) {
                 const unsigned long long m = S.msk[t];
                 if (m) {
                     S.base[t] = run;
-                    lastkey = (run / WIN_CUT) * 64 + t / SPAN_T;
+                    lastkey = win_key(run, rank, t);
                     run += popc64(m);
+                    rank++;
                 }
             }
-            const int carry = block_excl_max<SL_THREADS>(lastkey, s_tmp, -1);
+            const long long carry = block_excl_max<SL_THREADS>(lastkey, s_ltmp, -1ll);
             int nst = 0;
             {
-                int kk = carry;
+                long long kk = carry;
+                int rk = rank - ntl;
                 for (int t = lo; t < hi; t++)
                     if (S.msk[t]) {
-                        const int key = (S.base[t] / WIN_CUT) * 64 + t / SPAN_T;
+                        const long long key = win_key(S.base[t], rk++, t);
                         if (key != kk) nst++;
                         kk = key;
                     }
@@ -219,10 +282,11 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             int nwin;
             int pos = block_excl_sum<SL_THREADS>(nst, s_tmp, nwin);
             {
-                int kk = carry;
+                long long kk = carry;
+                int rk = rank - ntl;
                 for (int t = lo; t < hi; t++)
                     if (S.msk[t]) {
-                        const int key = (S.base[t] / WIN_CUT) * 64 + t / SPAN_T;
+                        const long long key = win_key(S.base[t], rk++, t);
                         if (key != kk) {
                             if (pos < SL_WL) {
                                 S.wl[pos] = S.base[t];
@@ -258,23 +322,28 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                 }
             }
             run_row = chunk_end;
+            tiles_row += chunk_tiles;
             __syncthreads();
         }
         if (threadIdx.x == 0 && run_row != nnz) set_err(&ctl->err, DERR_INTERNAL);
     }
 }
 
-void launch_structure(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol, Window *win,
-                      long long win_cap, Ctl *ctl, int nsm, cudaStream_t st) {
-    k_struct_ds<<<nsm * 4, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
-        A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol, win, win_cap, ctl);
+void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol,
+                      double *cval, Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+    auto kds = arith == 2 ? k_struct_ds<true> : k_struct_ds<false>;
+    kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
+        A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol, cval, win, win_cap, ctl);
     k_struct_l<<<nsm * 2, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol,
                                                             win, win_cap, ctl);
 }
 
 int configure_structure() {
-    int e = (int)cudaFuncSetAttribute(k_struct_ds, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    int e = (int)cudaFuncSetAttribute(k_struct_ds<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       SDS_WARPS * (int)sizeof(SdsSmem));
+    if (e) return e;
+    e = (int)cudaFuncSetAttribute(k_struct_ds<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  SDS_WARPS * (int)sizeof(SdsSmem));
     if (e) return e;
     return (int)cudaFuncSetAttribute(k_struct_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SlSmem));
 }

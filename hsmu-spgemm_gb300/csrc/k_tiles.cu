@@ -47,11 +47,13 @@ __global__ void __launch_bounds__(256) k_tiles(int K, const int *__restrict__ br
             if (lane == 0) tp = have_pend ? pend_t : -1;
             const bool head = valid && (t != tp);
             const unsigned heads = __ballot_sync(FULL, head);
+            const int nvalid = min(WARP, e - base);
             if (!FILL) {
                 run += __popc(heads);
+                pend_t = __shfl_sync(FULL, t, nvalid - 1);  // tile open at the end of this chunk
+                have_pend = true;
                 continue;
             }
-            const int nvalid = min(WARP, e - base);
             unsigned above = heads & ~((2u << lane) - 1u);
             if (lane == 31) above = 0;
             const int seg_end = above ? (__ffs(above) - 2) : (nvalid - 1);

@@ -34,7 +34,7 @@ STATUS = {0: "HSMU_OK", 1: "HSMU_ERR_INVALID", 2: "HSMU_ERR_ALLOC", 3: "HSMU_ERR
 # every symbol include/hsmu_gb.h declares (checked by the CPU test suite)
 EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_handle_destroy",
            "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_btiles_build", "hsmu_btiles_free",
-           "hsmu_csr_free", "hsmu_csr_download"]
+           "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul"]
 
 
 class HsmuError(RuntimeError):
@@ -66,7 +66,8 @@ class c_stats(ctypes.Structure):
                 ("ntiles_b", ctypes.c_int64), ("windows", ctypes.c_int64),
                 ("ms_convert", ctypes.c_float), ("ms_symbolic", ctypes.c_float),
                 ("ms_alloc", ctypes.c_float), ("ms_structure", ctypes.c_float),
-                ("ms_numeric", ctypes.c_float), ("ms_total", ctypes.c_float)]
+                ("ms_numeric", ctypes.c_float), ("ms_total", ctypes.c_float),
+                ("launches", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -98,6 +99,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     L.hsmu_btiles_free.argtypes = [ctypes.POINTER(c_btiles)]
     L.hsmu_csr_free.argtypes = [ctypes.POINTER(c_csr)]
     L.hsmu_csr_download.argtypes = [ctypes.POINTER(c_csr), P, P, P, P]
+    L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
     _lib = L
     return L
 
@@ -281,6 +283,14 @@ class Engine:
         _check(rc, "hsmu_spgemm")
         self.last_stats = st.as_dict() if stats else None
         return DeviceCSR(C)
+
+
+def selftest_dmul(n: int = 1 << 24, seed: int = 1) -> int:
+    """Mismatches of the integer-pipe multiply vs the FP64 pipe on n pairs (0 expected)."""
+    out = ctypes.c_uint64(0)
+    _check(load_library().hsmu_selftest_dmul(n, seed, ctypes.byref(out), _stream_ptr(None)),
+           "hsmu_selftest_dmul")
+    return int(out.value)
 
 
 def spgemm_host(A: CSR, B: CSR, engine: Engine | None = None, **kw) -> CSR:

@@ -82,7 +82,7 @@ typedef struct hsmu_btiles {
 /* Options; a NULL pointer means all defaults (zero-initialise to get them). */
 typedef struct hsmu_opts {
     int32_t validate;     /* 1: check A and B are canonical CSR before computing */
-    int32_t arith;        /* 0: auto (integer-pipe exact multiply mixed with FP64 pipe), 1: FP64 pipe only */
+    int32_t arith;        /* 0: FP64-pipe multiply (default), 2: exact integer-pipe multiply */
     int32_t window_cap;   /* 0: default slots per numeric window (<= 4096) */
     int32_t reserved[5];
 } hsmu_opts;
@@ -99,6 +99,8 @@ typedef struct hsmu_stats {
     float ms_structure;      /* column emission */
     float ms_numeric;        /* value accumulation */
     float ms_total;
+    int32_t launches;        /* kernels this call launched */
+    int32_t reserved;
 } hsmu_stats;
 
 typedef struct hsmu_handle_s *hsmu_handle;
@@ -137,6 +139,13 @@ int hsmu_csr_free(hsmu_csr *C);
  * row_ptr[M+1], col[nnz], val[nnz].  Stream-ordered; synchronizes `stream`
  * before returning. */
 int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream);
+
+/* Diagnostic: checks the numeric phase's integer-pipe FP64 multiply against
+ * the FP64 pipe's multiply on n generated operand pairs (all bit patterns,
+ * values in (-1,1), short significands with frequent ties) and stores the
+ * number of results that differ in any bit (expected 0).  No reference
+ * counterpart: the reference multiplies on the FP64 pipe only. */
+int hsmu_selftest_dmul(uint64_t n, uint64_t seed, uint64_t *mismatches, void *stream);
 
 #ifdef __cplusplus
 }

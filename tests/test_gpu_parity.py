@@ -184,4 +184,19 @@ def test_stats(engine):
     st = engine.last_stats
     assert st["products"] == gen.products(A, A)
     assert st["nnz_c"] == C.nnz
-    assert st["windows"] >= 1 and st["ms_total"] > 0
+    assert st["windows"] >= 0 and st["ms_total"] > 0 and st["launches"] >= 9
+
+
+def test_integer_pipe_multiply_selftest():
+    import hsmu_gb
+
+    assert hsmu_gb.selftest_dmul(1 << 24, seed=7) == 0
+
+
+@pytest.mark.parametrize("arith", [0, 2])
+def test_arith_modes_identical(engine, arith):
+    # FP64-pipe multiply (0) and integer-pipe multiply (2) give the same bits
+    for A in (gen.stencil27(8, 3, seed=1), gen.rmat(12, 16, seed=2, lo=-1.0, hi=1.0)):
+        C = run(engine, A, A, arith=arith)
+        rp, col, val = oracle.spgemm(A, A)
+        assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
