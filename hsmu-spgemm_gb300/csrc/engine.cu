@@ -20,7 +20,7 @@
 #include <cstring>
 #include <new>
 
-#include "../../include/hsmu_gb.h"
+#include "hsmu_gb.h"
 #include "hsmu_common.cuh"
 #include "hsmu_kernels.h"
 

@@ -76,11 +76,13 @@ class c_stats(ctypes.Structure):
 _lib = None
 
 
-def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
-    """Load libhsmu_gb.so (raises OSError if it was not built)."""
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load libhsmu_gb.so (raises OSError if it was not built).  HSMU_LIB in the
+    environment names an alternative build of the same library."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("HSMU_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise OSError("libhsmu_gb.so not built: run __graft_entry__.build() (missing %s)" % path)
     L = ctypes.CDLL(path)
