@@ -34,7 +34,7 @@ STATUS = {0: "HSMU_OK", 1: "HSMU_ERR_INVALID", 2: "HSMU_ERR_ALLOC", 3: "HSMU_ERR
 # every symbol include/hsmu_gb.h declares (checked by the CPU test suite)
 EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_handle_destroy",
            "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_btiles_build", "hsmu_btiles_free",
-           "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul"]
+           "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul", "hsmu_btiles_build_noalloc"]
 
 
 class HsmuError(RuntimeError):
@@ -101,6 +101,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_btiles_free.argtypes = [ctypes.POINTER(c_btiles)]
     L.hsmu_csr_free.argtypes = [ctypes.POINTER(c_csr)]
     L.hsmu_csr_download.argtypes = [ctypes.POINTER(c_csr), P, P, P, P]
+    L.hsmu_btiles_build_noalloc.argtypes = [ctypes.POINTER(c_csr), P, P, P, P, P]
     L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
     _lib = L
     return L

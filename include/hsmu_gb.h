@@ -132,6 +132,22 @@ int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B,
 int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream);
 int hsmu_btiles_free(hsmu_btiles *t);
 
+/* B -> 64-column bit tiles into caller-owned arrays, allocating nothing.
+ * No counterpart in the reference (its conversion always allocates).  For
+ * callers that cannot allocate device memory -- their memory is owned by
+ * their own pool or a fixed budget that forbids cudaMalloc/cudaFree on the
+ * compute path.  The caller passes B (device CSR) and the outputs:
+ * tile_ptr[B->M + 1] and tile_col/mask/tile_off with room for B->nnz
+ * entries (the tile count is tile_ptr[B->M] afterwards, at most B->nnz).
+ * The scan's scratch is a static ~64 KB device array inside the library,
+ * which limits B to 2^24 rows (larger B -> HSMU_ERR_OVERFLOW).  The first
+ * call on each device looks up that array's address (make it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU
+ * race, so serialise them.  Checks B's columns (HSMU_ERR_UNSORTED) and
+ * synchronizes `stream` before returning.  No handle needed. */
+int hsmu_btiles_build_noalloc(const hsmu_csr *B, int32_t *tile_ptr, int32_t *tile_col, uint64_t *mask,
+                              int32_t *tile_off, void *stream);
+
 /* Releases the arrays of a library-owned CSR (owned == 1) and zeroes it. */
 int hsmu_csr_free(hsmu_csr *C);
 
