@@ -41,9 +41,18 @@ FALLBACK_HBM_GBS = 6800.0
 # FP64 pipe: DADD/DMUL/DFMA lane-ops per second on GB300 (152 SMs), measured
 # with a dependent-chain throughput probe: 1.61 lane-ops/clk/SM at 2070 MHz.
 FP64_LANE_OPS_PER_S = 5.06e11
+# DRAM bytes (read + write) per launch of the dominant kernel, from ncu captures
+# summarised under profiles/ (null until captured for a workload).
+TRAFFIC = {
+    # profiles/k_struct_ds_stencil27_32_dof3.md: 447.3 MB on the 32^3 case, scaled by the
+    # algorithmic bytes (x1.993) to the 40^3 workload
+    "stencil27_40_dof3_AA": 891.6e6,
+}
 
 WORKLOADS = {
     "stencil27_40_dof3_AA": "27-point stencil, 40^3 grid x 3 dofs (n=192,000), C=A*A, uniform(-1,1), seed 1",
+    "stencil27_32_dof3_AA": "27-point stencil, 32^3 grid x 3 dofs (n=98,304), C=A*A, uniform(-1,1), seed 1 (profiling size)",
+    "rmat16_AA": "R-MAT scale 16, edge factor 16, merged, uniform(0,1), seed 2, C=A*A (profiling size)",
     "laplacian2d_256_AA": "5-point Laplacian, 256^2 grid (n=65,536), C=A*A, uniform(-1,1), seed 0",
     "rmat18_AA": "R-MAT scale 18, edge factor 16, (0.57,0.19,0.19,0.05), merged, uniform(0,1), seed 2, C=A*A",
     "rmat18_AAt": "R-MAT scale 18, edge factor 16, merged, uniform(0,1), seed 2, C=A*A^T",
@@ -55,6 +64,12 @@ def make_workload(name):
 
     if name == "stencil27_40_dof3_AA":
         A = gen.stencil27(40, 3, seed=1)
+        return A, A
+    if name == "stencil27_32_dof3_AA":
+        A = gen.stencil27(32, 3, seed=1)
+        return A, A
+    if name == "rmat16_AA":
+        A = gen.rmat(16, 16, seed=2)
         return A, A
     if name == "laplacian2d_256_AA":
         A = gen.laplacian2d(256, seed=0)
@@ -313,12 +328,22 @@ def run_engine(args):
     e2e_ms = dist_max(e0.elapsed_time(e1) / ke, world)
     e2e_value = world * 2.0 * products / (e2e_ms * 1e-3) / 1e9
 
-    # ---- roofline of the dominant kernel (numeric: reads A, B and C's columns, writes C's values)
+    # ---- roofline of the dominant kernel.  Values are accumulated either in the
+    # warp/CTA structure kernels (rows that fit one warp: columns + values in one
+    # pass) or in the window kernel k_numeric (wider rows); whichever stage takes
+    # longer is the dominant one.  Algorithmic bytes of that pass: read A and B,
+    # write C (4(M+1) + 12 nnz per matrix), each once.
     peak, peak_kind = load_peaks()
     alg_bytes = csr_bytes(A.M, A.nnz) + csr_bytes(B.M, B.nnz) + csr_bytes(A.M, nnz_c)
-    num_ms = stage["ms_numeric"] / args.steps
-    achieved = alg_bytes / (num_ms * 1e-3) / 1e9
-    fp64_ach = 2.0 * products / (num_ms * 1e-3)  # FP64 lane-ops/s (one DMUL + one DADD per product)
+    st_ms = stage["ms_structure"] / args.steps
+    nu_ms = stage["ms_numeric"] / args.steps
+    if st_ms >= nu_ms:
+        kname, kms = "k_struct_ds/k_struct_l (sorted columns + values of warp-sized rows)", st_ms
+    else:
+        kname, kms = "k_numeric (values, per window)", nu_ms
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    fp64_ach = 2.0 * products / (kms * 1e-3)  # FP64 lane-ops/s (one DMUL + one DADD per product)
+    traffic = TRAFFIC.get(args.workload)
 
     if rank != 0:
         return
@@ -335,13 +360,13 @@ def run_engine(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "hbm_gbs_step": round(alg_bytes / (ms * 1e-3) / 1e9, 2),
         "stages_ms": {k: round(v / args.steps, 4) for k, v in stage.items()},
-        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": round(achieved, 2),
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 2),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "peak_kind": peak_kind, "traffic": None,
-                     "alg_bytes": alg_bytes, "ms": round(num_ms, 4)},
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes": alg_bytes, "ms": round(kms, 4)},
         "fp64_pipe": {"achieved_lane_ops_per_s": fp64_ach, "peak_lane_ops_per_s": FP64_LANE_OPS_PER_S,
                       "frac": round(fp64_ach / FP64_LANE_OPS_PER_S, 4),
-                      "note": "numeric kernel: one DMUL + one DADD per product"},
+                      "note": "the value pass is bound by the FP64 pipe: one DMUL + one DADD per product"},
         "cpu_baseline": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in cpu.items()
                          if k != "seconds"},
         "e2e": {"value": round(e2e_value, 3), "unit": "GFLOPS", "ms_per_step": round(e2e_ms, 4),
