@@ -196,7 +196,7 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
     CK(palloc(&crp, (size_t)M + 1, st));
     launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
     // 3. exact count
-    launch_count(Ad, Btd, ri, ctl, h->nsm, st);
+    launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
     // 4. scan -> row_ptr, nnz
     launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
     CK(cudaGetLastError());
@@ -266,8 +266,8 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
         stats->ms_numeric = t;
         cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
         stats->ms_total = t;
-        // validate 2, tiles 5 (count, 3 scan, fill), bounds 1, count 2, scan 3, structure 2, numeric 1
-        stats->launches = (o.validate ? 2 : 0) + (Bt_in ? 0 : 5) + 6 + (hc.nnz > 0 ? 3 : 0);
+        // validate 2, tiles 5 (count, 3 scan, fill), bounds 1, count 3, scan 3, structure 3, numeric 1
+        stats->launches = (o.validate ? 2 : 0) + (Bt_in ? 0 : 5) + 7 + (hc.nnz > 0 ? 4 : 0);
     }
 done:
     pfree(ctl, st);

@@ -28,7 +28,7 @@ __device__ __forceinline__ int seg_of(int incl, int g) {
 // items, so one warp (first 0, stride 32) or all warps of a CTA
 // (first 32*w, stride 32*nwarps) keep every lane busy whatever the B row
 // lengths.  fn(tile_index) is called for valid items only.
-template <bool RESTRICT, class Fn>
+template <bool RESTRICT, bool NC = true, class Fn>
 __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, int stride,
                                                 const int *__restrict__ acol, const int *__restrict__ tptr,
                                                 const int *__restrict__ tcol, int c0, int c1, Fn fn) {
@@ -37,9 +37,9 @@ __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, i
         const int p = pb + lane;
         int lo = 0, hi = 0;
         if (p < a_hi) {
-            const int k = __ldg(acol + p);
-            lo = __ldg(tptr + k);
-            hi = __ldg(tptr + k + 1);
+            const int k = ldx<NC>(acol + p);
+            lo = ldx<NC>(tptr + k);
+            hi = ldx<NC>(tptr + k + 1);
             if (RESTRICT) {
                 lo = lower_bound_i32(tcol, lo, hi, c0);
                 hi = lower_bound_i32(tcol, lo, hi, c1);

@@ -37,9 +37,10 @@ constexpr int DCH_STRUCT = 8192;  // structure pass: 12 B per tile -> 96 KB
 
 // Row classes
 enum RowBin : int {
-    BIN_DS = 0,   // tile span <= SPAN_T : one warp, dense span table
-    BIN_L = 1,    // wider rows          : one CTA, dense chunked table
-    NBIN = 2
+    BIN_DS = 0,    // tile span <= SPAN_T : one warp, dense span table
+    BIN_L = 1,     // wider rows          : one CTA, dense chunked table
+    BIN_TINY = 2,  // <= TINY_MAX products: one thread, sorted insertion list
+    NBIN = 3
 };
 
 // device error bits (ctl->err)
@@ -96,6 +97,15 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 __device__ __forceinline__ int popc64(unsigned long long x) { return __popcll(x); }
+
+// Load through the read-only path (NC: data constant for the whole launch) or
+// through L2 only (!NC: data written earlier in the same launch by other
+// blocks, e.g. the first product of a batched Galerkin triple product).
+template <bool NC, class T>
+__device__ __forceinline__ T ldx(const T *p) {
+    if (NC) return __ldg(p);
+    return __ldcg(p);
+}
 
 // number of set bits of m strictly below bit b (0 <= b < 64)
 __device__ __forceinline__ int rank64(unsigned long long m, int b) {

@@ -48,7 +48,8 @@ size_t scan_tmp_ints(int n);
 void launch_scan(const int *in, int *out, int n, long long *total64, int *tmp, Ctl *ctl, cudaStream_t st);
 
 // k_symbolic.cu
-void launch_count(const DevCSR &A, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm, cudaStream_t st);
+void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
+                  cudaStream_t st);
 
 // k_structure.cu
 // writes C's columns and numeric windows; rows that fit one warp also get their values

@@ -30,7 +30,7 @@ __device__ __forceinline__ double prod_mul(double a, double b) {
 
 // SegFn:    void(int p, int k, int &elo, int &ehi)  -- called for valid lanes
 // LookupFn: int(int j) -> slot in acc, or -1 if j is not in the accumulator
-template <bool INT_MUL, class SegFn, class LookupFn>
+template <bool INT_MUL, bool NC = true, class SegFn, class LookupFn>
 __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *__restrict__ acol,
                                                 const double *__restrict__ aval, const int *__restrict__ brp,
                                                 const int *__restrict__ bcol, const double *__restrict__ bval,
@@ -41,8 +41,8 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
         int elo = 0, ehi = 0;
         double a = 0.0;
         if (p < a_hi) {
-            const int k = __ldg(acol + p);
-            a = __ldg(aval + p);
+            const int k = ldx<NC>(acol + p);
+            a = ldx<NC>(aval + p);
             seg(p, k, elo, ehi);
         }
         const int len = ehi - elo;
@@ -60,8 +60,8 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
             int j0 = 0;
             double b0 = 0.0;
             if (lane < ls) {
-                j0 = __ldg(bcol + es + lane);
-                b0 = __ldg(bval + es + lane);
+                j0 = ldx<NC>(bcol + es + lane);
+                b0 = ldx<NC>(bval + es + lane);
             }
             while (true) {
                 int n_off = off + WARP, n_es = es, n_ls = ls;
@@ -83,8 +83,8 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
                 int j1 = 0;
                 double b1 = 0.0;
                 if (have_next && n_off + lane < n_ls) {
-                    j1 = __ldg(bcol + n_es + n_off + lane);
-                    b1 = __ldg(bval + n_es + n_off + lane);
+                    j1 = ldx<NC>(bcol + n_es + n_off + lane);
+                    b1 = ldx<NC>(bval + n_es + n_off + lane);
                 }
                 if (off + lane < ls) {
                     const double pr = prod_mul<INT_MUL>(as, b0);
@@ -112,8 +112,8 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
         {
             const int e = __shfl_sync(FULL, elo, sg) + (lane - __shfl_sync(FULL, excl, sg));
             if (lane < total) {
-                j = __ldg(bcol + e);
-                b = __ldg(bval + e);
+                j = ldx<NC>(bcol + e);
+                b = ldx<NC>(bval + e);
             }
         }
         for (int f = 0; f < total; f += WARP) {
@@ -126,8 +126,8 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
                 const int e = __shfl_sync(FULL, elo, sg_n) + (gn - __shfl_sync(FULL, excl, sg_n));
                 as_n = __shfl_sync(FULL, a, sg_n);
                 if (gn < total) {
-                    j_n = __ldg(bcol + e);
-                    b_n = __ldg(bval + e);
+                    j_n = ldx<NC>(bcol + e);
+                    b_n = ldx<NC>(bval + e);
                 }
             }
             int slot = -1 - lane;

@@ -1,0 +1,201 @@
+// Per-row routines for rows with few intermediate products ("tiny" rows:
+// at most TINY_MAX products), one thread per row.
+//
+// The AMG Galerkin operands (A*P: <= 7 products per row, P^T*(AP): <= 32)
+// and the 2-D Laplacian (<= 25) consist of such rows only; a warp per row
+// would leave most lanes idle.  A thread walks its row's products in the
+// oracle's order (A entry, then B entry), keeping the distinct columns in a
+// small sorted list (insertion), so the count pass and the fill pass need no
+// B tiles and no sorting afterwards.  In the fill pass every product is added
+// to its column's accumulator in that same order: 0.0 + p_1 + p_2 + ...,
+// each p rounded before the add, bit-identical to the host oracle.
+//
+// The per-thread lists live in shared memory laid out element-major
+// ([TINY_MAX][threads]) so that neighbouring threads hit neighbouring banks.
+#pragma once
+#include "hsmu_common.cuh"
+
+namespace hsmu {
+
+constexpr int TINY_MAX = 32;
+
+// number of distinct columns of row (a_lo..a_hi) of A*B; -1 if the row has
+// more than TINY_MAX products (caller classified it wrongly).
+template <bool NC = true>
+__device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__restrict__ acol,
+                                              const int *__restrict__ brp, const int *__restrict__ bcol, int *cols,
+                                              int stride) {
+    int n = 0, seen = 0;
+    for (int p = a_lo; p < a_hi; p++) {
+        const int k = ldx<NC>(acol + p);
+        const int qe = ldx<NC>(brp + k + 1);
+        for (int q = ldx<NC>(brp + k); q < qe; q++) {
+            if (++seen > TINY_MAX) return -1;
+            const int j = ldx<NC>(bcol + q);
+            int pos = n;
+            while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
+            if (pos > 0 && cols[(pos - 1) * stride] == j) continue;
+            for (int t = n; t > pos; t--) cols[t * stride] = cols[(t - 1) * stride];
+            cols[pos * stride] = j;
+            n++;
+        }
+    }
+    return n;
+}
+
+// fills C's columns and values of the row at out_col/out_val (nnz entries
+// expected); returns false on an inconsistency (count mismatch / overflow).
+template <bool NC = true, class MulFn>
+__device__ __forceinline__ bool tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
+                                              const double *__restrict__ aval, const int *__restrict__ brp,
+                                              const int *__restrict__ bcol, const double *__restrict__ bval,
+                                              int *cols, double *acc, int stride, int nnz, int *__restrict__ out_col,
+                                              double *__restrict__ out_val, MulFn mul) {
+    int n = 0, seen = 0;
+    for (int p = a_lo; p < a_hi; p++) {
+        const int k = ldx<NC>(acol + p);
+        const double a = ldx<NC>(aval + p);
+        const int qe = ldx<NC>(brp + k + 1);
+        for (int q = ldx<NC>(brp + k); q < qe; q++) {
+            if (++seen > TINY_MAX) return false;
+            const int j = ldx<NC>(bcol + q);
+            const double pr = mul(a, ldx<NC>(bval + q));
+            int pos = n;
+            while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
+            if (pos > 0 && cols[(pos - 1) * stride] == j) {
+                acc[(pos - 1) * stride] = __dadd_rn(acc[(pos - 1) * stride], pr);
+                continue;
+            }
+            for (int t = n; t > pos; t--) {
+                cols[t * stride] = cols[(t - 1) * stride];
+                acc[t * stride] = acc[(t - 1) * stride];
+            }
+            cols[pos * stride] = j;
+            acc[pos * stride] = __dadd_rn(0.0, pr);
+            n++;
+        }
+    }
+    if (n != nnz) return false;
+    for (int t = 0; t < n; t++) {
+        out_col[t] = cols[t * stride];
+        out_val[t] = acc[t * stride];
+    }
+    return true;
+}
+
+}  // namespace hsmu
+
+#include "hsmu_block.cuh"
+#include "hsmu_products.cuh"
+
+namespace hsmu {
+
+// ---------------------------------------------------------------------------
+// Warp-per-row routines on a dense span table, driven by B's entries (no B
+// tiles): used by the batched engine, where B may be produced inside the same
+// launch.  msk[] holds SPAN_T u64 masks, base[] SPAN_T ints, acc[] `cap`
+// doubles, all private to the warp.
+
+// first and last column of row (a_lo..a_hi) of A*B: min/max over the first /
+// last entries of the referenced (sorted) B rows; returns products too.
+template <bool NC = true>
+__device__ __forceinline__ void warp_row_extent(int a_lo, int a_hi, const int *__restrict__ acol,
+                                                const int *__restrict__ brp, const int *__restrict__ bcol,
+                                                int &cmin, int &cmax, int &prod) {
+    cmin = 0x7fffffff;
+    cmax = -1;
+    prod = 0;
+    for (int p = a_lo + lane_id(); p < a_hi; p += WARP) {
+        const int k = ldx<NC>(acol + p);
+        const int s = ldx<NC>(brp + k), e = ldx<NC>(brp + k + 1);
+        if (e > s) {
+            cmin = min(cmin, ldx<NC>(bcol + s));
+            cmax = max(cmax, ldx<NC>(bcol + e - 1));
+            prod += e - s;
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        cmin = min(cmin, __shfl_xor_sync(FULL, cmin, d));
+        cmax = max(cmax, __shfl_xor_sync(FULL, cmax, d));
+        prod += __shfl_xor_sync(FULL, prod, d);
+    }
+}
+
+// OR the row's columns into msk[0..span) (tile t0 + i at msk[i]); false on a column outside the span
+template <bool NC = true>
+__device__ __forceinline__ bool warp_row_masks(int a_lo, int a_hi, const int *__restrict__ acol,
+                                               const int *__restrict__ brp, const int *__restrict__ bcol, int t0,
+                                               int span, unsigned long long *msk) {
+    for (int t = lane_id(); t < span; t += WARP) msk[t] = 0ull;
+    __syncwarp();
+    bool bad = false;
+    warp_walk_tiles<false, NC>(a_lo, a_hi, 0, WARP, acol, brp, bcol, 0, 0, [&](int q) {
+        const int j = ldx<NC>(bcol + q);
+        const int t = (j >> 6) - t0;
+        if (t >= 0 && t < span) atomicOr(msk + t, 1ull << (j & 63));
+        else bad = true;
+    });
+    __syncwarp();
+    return !__any_sync(FULL, bad);
+}
+
+// nnz of the masks
+__device__ __forceinline__ int warp_mask_count(const unsigned long long *msk, int span) {
+    int c = 0;
+    for (int t = lane_id(); t < span; t += WARP) c += popc64(msk[t]);
+    return warp_sum(c);
+}
+
+// Given the row's masks: write its sorted columns to out_col, accumulate the
+// products (oracle order) in acc and write the values to out_val.  nnz must
+// equal the masks' popcount and be <= cap.  Returns false on inconsistency.
+template <bool INT_MUL, bool NC = true>
+__device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
+                                              const double *__restrict__ aval, const int *__restrict__ brp,
+                                              const int *__restrict__ bcol, const double *__restrict__ bval,
+                                              int t0, int span, const unsigned long long *msk, int *base,
+                                              double *acc, int nnz, int *__restrict__ out_col,
+                                              double *__restrict__ out_val) {
+    const int lane = lane_id();
+    const int per = (span + WARP - 1) / WARP;
+    const int lo = min(span, lane * per), hi = min(span, lo + per);
+    int sum = 0;
+    for (int t = lo; t < hi; t++) sum += popc64(msk[t]);
+    const int incl = warp_incl_scan(sum);
+    if (__shfl_sync(FULL, incl, WARP - 1) != nnz) return false;
+    int run = incl - sum;
+    for (int t = lo; t < hi; t++) {
+        unsigned long long m = msk[t];
+        base[t] = run;
+        int pos = run;
+        const int cb = (t0 + t) << 6;
+        run += popc64(m);
+        while (m) {
+            out_col[pos++] = cb + (__ffsll((long long)m) - 1);
+            m &= m - 1ull;
+        }
+    }
+    for (int q = lane; q < nnz; q += WARP) acc[q] = 0.0;
+    __syncwarp();
+    auto seg = [&](int, int k, int &elo, int &ehi) {
+        elo = ldx<NC>(brp + k);
+        ehi = ldx<NC>(brp + k + 1);
+    };
+    auto lookup = [&](int j) -> int {
+        const int t = (j >> 6) - t0;
+        if ((unsigned)t >= (unsigned)span) return -1;
+        const unsigned long long m = msk[t];
+        const int bit = j & 63;
+        if (!((m >> bit) & 1ull)) return -1;
+        return base[t] + rank64(m, bit);
+    };
+    bool bad = false;
+    warp_accumulate<INT_MUL, NC>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, acc, bad);
+    __syncwarp();
+    for (int q = lane; q < nnz; q += WARP) out_val[q] = acc[q];
+    __syncwarp();
+    return !__any_sync(FULL, bad);
+}
+
+}  // namespace hsmu

@@ -18,6 +18,7 @@
 
 #include "hsmu_common.cuh"
 #include "hsmu_kernels.h"
+#include "hsmu_rowops.cuh"
 
 namespace hsmu {
 
@@ -63,7 +64,7 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                 ri.cnnz[i] = 0;
             } else {
                 const int span = tmax - tmin + 1;
-                bin = span <= SPAN_T ? BIN_DS : BIN_L;
+                bin = prod <= TINY_MAX ? BIN_TINY : (span <= SPAN_T ? BIN_DS : BIN_L);
                 lpos = atomicAdd(&s_cnt[bin], 1);
                 my_prod += (unsigned long long)prod;
                 const long long cap = prod < (long long)N ? prod : (long long)N;

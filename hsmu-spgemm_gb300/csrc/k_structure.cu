@@ -25,6 +25,7 @@
 #include "hsmu_block.cuh"
 #include "hsmu_kernels.h"
 #include "hsmu_products.cuh"
+#include "hsmu_rowops.cuh"
 
 namespace hsmu {
 
@@ -329,8 +330,38 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
     }
 }
 
+constexpr int TINYF_THREADS = 128;
+
+// tiny rows: one thread per row writes its sorted columns and values
+template <bool INT_MUL>
+__global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *__restrict__ arp,
+                                                             const int *__restrict__ acol,
+                                                             const double *__restrict__ aval,
+                                                             const int *__restrict__ brp,
+                                                             const int *__restrict__ bcol,
+                                                             const double *__restrict__ bval, RowInfo ri,
+                                                             const int *__restrict__ crp, int *__restrict__ ccol,
+                                                             double *__restrict__ cval, Ctl *ctl) {
+    __shared__ int s_cols[TINY_MAX * TINYF_THREADS];
+    __shared__ double s_acc[TINY_MAX * TINYF_THREADS];
+    const int n = ctl->bin_count[BIN_TINY];
+    const int *rows = ri.bins + (size_t)BIN_TINY * M;
+    bool bad = false;
+    for (int r = blockIdx.x * TINYF_THREADS + threadIdx.x; r < n; r += gridDim.x * TINYF_THREADS) {
+        const int i = rows[r];
+        const int c0 = crp[i];
+        if (!tiny_row_fill(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, s_cols + threadIdx.x,
+                           s_acc + threadIdx.x, TINYF_THREADS, crp[i + 1] - c0, ccol + c0, cval + c0,
+                           [](double x, double y) { return prod_mul<INT_MUL>(x, y); }))
+            bad = true;
+    }
+    if (bad) set_err(&ctl->err, DERR_INTERNAL);
+}
+
 void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol,
                       double *cval, Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+    auto kt = arith == 2 ? k_fill_tiny<true> : k_fill_tiny<false>;
+    kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, crp, ccol, cval, ctl);
     auto kds = arith == 2 ? k_struct_ds<true> : k_struct_ds<false>;
     kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
         A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol, cval, win, win_cap, ctl);

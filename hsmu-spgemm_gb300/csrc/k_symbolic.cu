@@ -16,6 +16,7 @@
 // B tile) sequence, 32 lanes busy regardless of row lengths.
 #include "hsmu_block.cuh"
 #include "hsmu_kernels.h"
+#include "hsmu_rowops.cuh"
 
 namespace hsmu {
 
@@ -107,7 +108,29 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
     }
 }
 
-void launch_count(const DevCSR &A, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm, cudaStream_t st) {
+constexpr int TINY_THREADS = 256;
+
+// tiny rows: one thread per row, distinct columns counted by sorted insertion
+__global__ void __launch_bounds__(TINY_THREADS) k_count_tiny(int M, const int *__restrict__ arp,
+                                                             const int *__restrict__ acol,
+                                                             const int *__restrict__ brp,
+                                                             const int *__restrict__ bcol, RowInfo ri, Ctl *ctl) {
+    __shared__ int s_cols[TINY_MAX * TINY_THREADS];
+    const int n = ctl->bin_count[BIN_TINY];
+    const int *rows = ri.bins + (size_t)BIN_TINY * M;
+    bool bad = false;
+    for (int r = blockIdx.x * TINY_THREADS + threadIdx.x; r < n; r += gridDim.x * TINY_THREADS) {
+        const int i = rows[r];
+        const int c = tiny_row_count(arp[i], arp[i + 1], acol, brp, bcol, s_cols + threadIdx.x, TINY_THREADS);
+        if (c < 0) bad = true;
+        ri.cnnz[i] = c < 0 ? 0 : c;
+    }
+    if (bad) set_err(&ctl->err, DERR_INTERNAL);
+}
+
+void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
+                  cudaStream_t st) {
+    k_count_tiny<<<nsm * 4, TINY_THREADS, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, ri, ctl);
     k_count_ds<<<nsm * 6, DS_WARPS * 32, 0, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, ctl);
     k_count_l<<<nsm * 3, L_THREADS, DCH_COUNT * sizeof(unsigned long long), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col,
                                                                                    Bt.mask, ri, ctl);

@@ -29,12 +29,16 @@ LIB_PATH = os.path.join(PKG, "libhsmu_gb.so")
 HSMU_OK = 0
 STATUS = {0: "HSMU_OK", 1: "HSMU_ERR_INVALID", 2: "HSMU_ERR_ALLOC", 3: "HSMU_ERR_CUDA",
           4: "HSMU_ERR_OVERFLOW", 5: "HSMU_ERR_UNSORTED", 6: "HSMU_ERR_INTERNAL",
-          7: "HSMU_ERR_TIMEOUT", 8: "HSMU_ERR_NO_DEVICE"}
+          7: "HSMU_ERR_TIMEOUT", 8: "HSMU_ERR_NO_DEVICE", 9: "HSMU_ERR_UNSUPPORTED"}
+BATCH_PRODUCT, BATCH_GALERKIN = 0, 1
 
 # every symbol include/hsmu_gb.h declares (checked by the CPU test suite)
 EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_handle_destroy",
            "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_btiles_build", "hsmu_btiles_free",
-           "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul", "hsmu_btiles_build_noalloc"]
+           "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul", "hsmu_btiles_build_noalloc",
+           "hsmu_batch_create", "hsmu_batch_execute", "hsmu_batch_graph_launch", "hsmu_batch_status",
+           "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
+           "hsmu_gen_poisson7", "hsmu_gen_aggregation"]
 
 
 class HsmuError(RuntimeError):
@@ -102,6 +106,18 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_csr_free.argtypes = [ctypes.POINTER(c_csr)]
     L.hsmu_csr_download.argtypes = [ctypes.POINTER(c_csr), P, P, P, P]
     L.hsmu_btiles_build_noalloc.argtypes = [ctypes.POINTER(c_csr), P, P, P, P, P]
+    L.hsmu_batch_create.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
+                                    ctypes.POINTER(c_csr), ctypes.POINTER(c_opts), ctypes.POINTER(P), P]
+    L.hsmu_batch_execute.argtypes = [P, P]
+    L.hsmu_batch_graph_launch.argtypes = [P, P]
+    L.hsmu_batch_status.argtypes = [P, P]
+    L.hsmu_batch_result.argtypes = [P, ctypes.c_int, ctypes.POINTER(c_csr)]
+    L.hsmu_batch_set_params.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.hsmu_batch_autotune.argtypes = [P, P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_float)]
+    L.hsmu_batch_destroy.argtypes = [P]
+    L.hsmu_gen_poisson7.argtypes = [ctypes.c_int, ctypes.POINTER(c_csr), P]
+    L.hsmu_gen_aggregation.argtypes = [ctypes.c_int, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), P]
     L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
     _lib = L
     return L
@@ -286,6 +302,75 @@ class Engine:
         _check(rc, "hsmu_spgemm")
         self.last_stats = st.as_dict() if stats else None
         return DeviceCSR(C)
+
+
+class Batch:
+    """Many products in one persistent launch (hsmu_batch_*).
+
+    kind BATCH_PRODUCT: C_p = A[p] * B[p]; BATCH_GALERKIN: C_p = Pt[p] * (A[p] * B[p]).
+    Results are views into the batch's output pool (valid while the batch lives)."""
+
+    def __init__(self, engine: "Engine", kind: int, A, B, Pt=None, arith: int = 0, stream=None):
+        n = len(A)
+        self._keep = (list(A), list(B), list(Pt) if Pt is not None else None)
+        arrA = (c_csr * n)(*[x.desc for x in A])
+        arrB = (c_csr * n)(*[x.desc for x in B])
+        arrP = (c_csr * n)(*[x.desc for x in Pt]) if Pt is not None else None
+        o = c_opts(0, int(arith), 0)
+        h = ctypes.c_void_p()
+        _check(load_library().hsmu_batch_create(engine.handle, kind, n, arrA, arrB, arrP, ctypes.byref(o),
+                                                ctypes.byref(h), _stream_ptr(stream)), "hsmu_batch_create")
+        self.handle = h
+        self.n = n
+
+    def execute(self, stream=None):
+        _check(load_library().hsmu_batch_execute(self.handle, _stream_ptr(stream)), "hsmu_batch_execute")
+
+    def graph_launch(self, stream=None):
+        _check(load_library().hsmu_batch_graph_launch(self.handle, _stream_ptr(stream)), "hsmu_batch_graph_launch")
+
+    def status(self, stream=None):
+        _check(load_library().hsmu_batch_status(self.handle, _stream_ptr(stream)), "hsmu_batch_status")
+
+    def set_params(self, tiny: int, grid: int = 0):
+        _check(load_library().hsmu_batch_set_params(self.handle, tiny, grid), "hsmu_batch_set_params")
+
+    def autotune(self, stream=None):
+        t, g, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _check(load_library().hsmu_batch_autotune(self.handle, _stream_ptr(stream), ctypes.byref(t),
+                                                  ctypes.byref(g), ctypes.byref(ms)), "hsmu_batch_autotune")
+        return t.value, g.value, ms.value
+
+    def result(self, p: int) -> "DeviceCSR":
+        C = c_csr()
+        _check(load_library().hsmu_batch_result(self.handle, p, ctypes.byref(C)), "hsmu_batch_result")
+        return DeviceCSR(C, keep=self)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load_library().hsmu_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def gen_poisson7(side: int, stream=None) -> "DeviceCSR":
+    """7-point Poisson matrix of a side^3 grid generated on the device (owned)."""
+    C = c_csr()
+    _check(load_library().hsmu_gen_poisson7(side, ctypes.byref(C), _stream_ptr(stream)), "hsmu_gen_poisson7")
+    return DeviceCSR(C)
+
+
+def gen_aggregation(side: int, stream=None):
+    """(P, P^T) of the 2x2x2 aggregation of a side^3 grid, generated on the device (owned)."""
+    P, Pt = c_csr(), c_csr()
+    _check(load_library().hsmu_gen_aggregation(side, ctypes.byref(P), ctypes.byref(Pt), _stream_ptr(stream)),
+           "hsmu_gen_aggregation")
+    return DeviceCSR(P), DeviceCSR(Pt)
 
 
 def selftest_dmul(n: int = 1 << 24, seed: int = 1) -> int:

@@ -45,7 +45,8 @@ typedef enum hsmu_status {
     HSMU_ERR_UNSORTED = 5,     /* validation: columns not strictly increasing / out of range */
     HSMU_ERR_INTERNAL = 6,     /* a device-side consistency check failed */
     HSMU_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up */
-    HSMU_ERR_NO_DEVICE = 8     /* no usable sm_103 device */
+    HSMU_ERR_NO_DEVICE = 8,    /* no usable sm_103 device */
+    HSMU_ERR_UNSUPPORTED = 9   /* a batch holds rows that need the plain engine's large-row path */
 } hsmu_status;
 
 /* CSR matrix descriptor.  row_ptr has M+1 entries, col/val have nnz entries.
@@ -155,6 +156,43 @@ int hsmu_csr_free(hsmu_csr *C);
  * row_ptr[M+1], col[nnz], val[nnz].  Stream-ordered; synchronizes `stream`
  * before returning. */
 int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream);
+
+/* ---- Batched persistent engine ------------------------------------------
+ * Many independent products in ONE cooperative persistent launch, with no
+ * host synchronisation inside and outputs in one preallocated pool:
+ *   HSMU_BATCH_PRODUCT : C_p = A[p] * B[p]
+ *   HSMU_BATCH_GALERKIN: C_p = Pt[p] * (A[p] * B[p])   (B = prolongator P, Pt = P^T)
+ * No counterpart in the reference, which runs products one by one
+ * (src/NHC_spgemm.cuh:7 per product).  hsmu_batch_create sizes the pool with
+ * one device pass and one host read; execute / graph_launch only enqueue
+ * work (graph_launch captures the launch in a CUDA graph on first use and
+ * replays it).  Results (hsmu_batch_result) are descriptors into the pool
+ * (owned = 0) valid until hsmu_batch_destroy; rows of every product must fit
+ * the warp path (tile span <= 512 tiles, <= 512 entries), otherwise
+ * hsmu_batch_status reports HSMU_ERR_UNSUPPORTED. */
+#define HSMU_BATCH_PRODUCT 0
+#define HSMU_BATCH_GALERKIN 1
+typedef struct hsmu_batch_s *hsmu_batch;
+int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const hsmu_csr *B, const hsmu_csr *Pt,
+                      const hsmu_opts *opts, hsmu_batch *out, void *stream);
+int hsmu_batch_execute(hsmu_batch b, void *stream);
+int hsmu_batch_graph_launch(hsmu_batch b, void *stream);
+/* synchronizes `stream`; maps the device-side error bits to a status */
+int hsmu_batch_status(hsmu_batch b, void *stream);
+int hsmu_batch_result(hsmu_batch b, int p, hsmu_csr *C);
+/* tiny: products threshold of the thread-per-row class (0..32); grid: blocks (0 = keep) */
+int hsmu_batch_set_params(hsmu_batch b, int tiny, int grid);
+/* times the parameter candidates on this batch and keeps the fastest */
+int hsmu_batch_autotune(hsmu_batch b, void *stream, int *best_tiny, int *best_grid, float *best_ms);
+int hsmu_batch_destroy(hsmu_batch b);
+
+/* ---- Synthetic AMG operators generated on the device (workload inputs) ---
+ * 7-point Poisson matrix of a side^3 grid (6 on the diagonal, -1 off it, natural
+ * ordering) and the piecewise-constant 2x2x2 aggregation prolongator P (fine x
+ * ceil(side/2)^3, weight 1) with its transpose.  Outputs are library-owned
+ * (free with hsmu_csr_free).  No counterpart in the reference. */
+int hsmu_gen_poisson7(int side, hsmu_csr *A, void *stream);
+int hsmu_gen_aggregation(int side, hsmu_csr *P, hsmu_csr *Pt, void *stream);
 
 /* Diagnostic: checks the numeric phase's integer-pipe FP64 multiply against
  * the FP64 pipe's multiply on n generated operand pairs (all bit patterns,

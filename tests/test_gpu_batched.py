@@ -1,0 +1,102 @@
+"""Batched persistent engine (hsmu_batch_*) and the device AMG generators.
+
+The batch must give, product by product, exactly what the oracle gives (the
+same summation order), through plain launches, CUDA-graph replays and after
+autotuning; rows it cannot take are reported, not computed wrongly."""
+import numpy as np
+import pytest
+
+import oracle
+from hsmu_gb import gen
+
+pytestmark = pytest.mark.gpu
+
+
+def host(d):
+    return d.to_host()
+
+
+@pytest.mark.parametrize("side", [1, 2, 5, 8, 13])
+def test_device_generators_match_host(side):
+    import hsmu_gb
+
+    A = host(hsmu_gb.gen_poisson7(side))
+    ref = gen.poisson7(side)
+    np.testing.assert_array_equal(A.row_ptr, ref.row_ptr)
+    np.testing.assert_array_equal(A.col, ref.col)
+    np.testing.assert_array_equal(A.val, ref.val)
+    dP, dPt = hsmu_gb.gen_aggregation(side)
+    P, Pt = host(dP), host(dPt)
+    Pr = gen.aggregation_prolongator(side)
+    np.testing.assert_array_equal(P.row_ptr, Pr.row_ptr)
+    np.testing.assert_array_equal(P.col, Pr.col)
+    T = gen.transpose(Pr)
+    np.testing.assert_array_equal(Pt.row_ptr, T.row_ptr)
+    np.testing.assert_array_equal(Pt.col, T.col)
+    assert P.N == Pt.M == ((side + 1) // 2) ** 3
+
+
+def galerkin_oracle(A, P, Pt):
+    rp, col, val = oracle.spgemm(A, P)
+    AP = gen.CSR(A.M, P.N, rp.astype(np.int32), col, val)
+    return oracle.spgemm(Pt, AP)
+
+
+def test_galerkin_batch_matches_oracle(engine):
+    import hsmu_gb
+
+    sides = [3, 16, 5, 24, 9, 2, 31]
+    As, Ps, Pts = [], [], []
+    for s in sides:
+        As.append(hsmu_gb.gen_poisson7(s))
+        P, Pt = hsmu_gb.gen_aggregation(s)
+        Ps.append(P)
+        Pts.append(Pt)
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_GALERKIN, As, Ps, Pts)
+    for launch in ("execute", "graph", "graph"):
+        b.execute() if launch == "execute" else b.graph_launch()
+        b.status()
+        for p, s in enumerate(sides):
+            C = host(b.result(p))
+            rp, col, val = galerkin_oracle(host(As[p]), host(Ps[p]), host(Pts[p]))
+            np.testing.assert_array_equal(C.row_ptr, rp.astype(np.int32))
+            np.testing.assert_array_equal(C.col, col)
+            assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+    tiny, grid, ms = b.autotune()
+    assert 0 < tiny <= 32 and grid > 0 and ms > 0
+    b.graph_launch()
+    b.status()
+    C = host(b.result(3))
+    rp, col, val = galerkin_oracle(host(As[3]), host(Ps[3]), host(Pts[3]))
+    assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
+def test_product_batch_matches_plain(engine):
+    import hsmu_gb
+
+    mats = [gen.laplacian2d(40, seed=1), gen.poisson_random(3000, 3, seed=2, ncols=3000),
+            gen.stencil27(7, 3, seed=3), gen.laplacian2d(9, seed=4)]
+    dA = [hsmu_gb.DeviceCSR.from_host(m) for m in mats]
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_PRODUCT, dA, dA)
+    for tiny in (0, 8, 32):  # 0: every row through the warp path
+        b.set_params(tiny)
+        b.execute()
+        b.status()
+        for p, m in enumerate(mats):
+            C = host(b.result(p))
+            rp, col, val = oracle.spgemm(m, m)
+            np.testing.assert_array_equal(C.row_ptr, rp.astype(np.int32))
+            np.testing.assert_array_equal(C.col, col)
+            assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
+def test_batch_reports_unsupported_rows(engine):
+    import hsmu_gb
+
+    big = gen.rmat(12, 16, seed=2)  # rows wider than the warp path
+    d = hsmu_gb.DeviceCSR.from_host(big)
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_PRODUCT, [d], [d])
+    b.execute()
+    with pytest.raises(hsmu_gb.HsmuError) as ei:
+        b.status()
+    assert ei.value.status == 9
