@@ -188,10 +188,10 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
                 const long long o = R.excl[i];
                 const int nnz = R.cnnz[i];
                 if (o + nnz <= R.cap) {
-                    const bool ok = tiny_row_fill<NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val, S.t.cols + lane,
-                                                  S.t.acc + lane, WARP, nnz, R.col_pool + o, R.val_pool + o,
-                                                  [](double x, double y) { return prod_mul<INT_MUL>(x, y); });
-                    if (!ok) atomicOr(P.err, BERR_INTERNAL);
+                    const int got = tiny_row_fill<NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val, S.t.cols + lane,
+                                                      S.t.acc + lane, WARP, nnz, R.col_pool + o, R.val_pool + o,
+                                                      [](double x, double y) { return prod_mul<INT_MUL>(x, y); });
+                    if (got != nnz) atomicOr(P.err, BERR_INTERNAL);
                 }
             }
         }

@@ -223,10 +223,12 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
     if (stats) cudaEventRecord(h->ev[3], st);
 
     // 5a. structure + windows
-    if (hc.nnz > 0) launch_structure(Ad, Bd, Btd, ri, crp, ccol, cval, win, win_cap, ctl, o.arith, h->nsm, st);
+    if (hc.nnz > 0)
+        launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_PLAIN, crp, nullptr, ccol, cval, nullptr, nullptr}, win, win_cap,
+                         ctl, o.arith, h->nsm, st);
     if (stats) cudaEventRecord(h->ev[4], st);
     // 5b. values
-    if (hc.nnz > 0) launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, ctl, o.arith, h->nsm, st);
+    if (hc.nnz > 0) launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, nullptr, ctl, o.arith, h->nsm, st);
     CK(cudaGetLastError());
     if (stats) cudaEventRecord(h->ev[5], st);
 
@@ -287,6 +289,221 @@ done:
     pfree(crp, st);
     pfree(ccol, st);
     pfree(cval, st);
+    if (rc != HSMU_OK) cudaStreamSynchronize(st);
+    return rc;
+}
+
+// Learned path (see learned.cu): predicted slots instead of the exact count pass.
+int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
+                        const hsmu_opts *opts, cudaStream_t st, hsmu_stats *stats) {
+    if (!h || !csr_ok(A) || !csr_ok(B) || !C || !model || !model->params) return HSMU_ERR_INVALID;
+    if (A->N != B->M) return HSMU_ERR_INVALID;
+    hsmu_opts o{};
+    if (opts) o = *opts;
+    const int M = A->M;
+    int rc = HSMU_OK;
+    Ctl *ctl = nullptr;
+    hsmu_btiles bt{};
+    RowInfo ri{};
+    int *scan_tmp = nullptr, *cap = nullptr, *crp = nullptr, *ccol = nullptr, *scol = nullptr;
+    long long *soff = nullptr;
+    float4 *feat = nullptr;
+    unsigned char *flag = nullptr;
+    double *cval = nullptr, *sval = nullptr;
+    Window *win = nullptr;
+    long long win_cap = 0, spec_total = 0;
+    Ctl hc{};
+    DevCSR Ad = dev(A), Bd = dev(B);
+    DevTiles Btd{};
+    std::memset(C, 0, sizeof(*C));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        cudaEventRecord(h->ev[0], st);
+    }
+    CK(palloc(&ctl, 1, st));
+    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    if (o.validate) {
+        launch_validate(Ad, ctl, grid_rows(h), st);
+        launch_validate(Bd, ctl, grid_rows(h), st);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (h->h_ctl->err) {
+            rc = err_from_dev(h->h_ctl->err);
+            goto done;
+        }
+    }
+    rc = build_tiles(h, B, &bt, ctl, 0, st, stats != nullptr);
+    if (rc) goto done;
+    Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
+    if (stats) cudaEventRecord(h->ev[1], st);
+    CK(palloc(&ri.prod, (size_t)M, st));
+    CK(palloc(&ri.tmin, (size_t)M, st));
+    CK(palloc(&ri.tmax, (size_t)M, st));
+    CK(palloc(&ri.bins, (size_t)M * NBIN, st));
+    CK(palloc(&ri.cnnz, (size_t)M + 1, st));
+    CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
+    CK(palloc(&feat, (size_t)M, st));
+    CK(palloc(&cap, (size_t)M + 1, st));
+    CK(palloc(&soff, (size_t)M + 1, st));
+    CK(palloc(&flag, (size_t)M, st));
+    CK(cudaMemsetAsync(flag, 0, (size_t)M, st));
+    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
+    launch_features(Ad, Bd, feat, nullptr, h->nsm, st);
+    launch_capacity(model->params, feat, ri.prod, M, B->N, model->margin, cap, h->nsm, st);
+    launch_scan64(cap, soff, M, &ctl->nnz, scan_tmp, st);  // nnz field holds the slot total for now
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (stats) cudaEventRecord(h->ev[2], st);
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        goto done;
+    }
+    spec_total = hc.nnz;
+    win_cap = 2 * (long long)hc.win_bound;  // speculative pass + redo of overflowing rows
+    if (win_cap > INT_MAX) {
+        rc = HSMU_ERR_OVERFLOW;
+        goto done;
+    }
+    CK(palloc(&scol, (size_t)spec_total, st));
+    CK(palloc(&sval, (size_t)spec_total, st));
+    CK(palloc(&win, (size_t)win_cap, st));
+    CK(palloc(&crp, (size_t)M + 1, st));
+    if (stats) cudaEventRecord(h->ev[3], st);
+    // structure (+ values of warp-sized rows) into the slots; exact counts found here
+    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag}, win, win_cap, ctl,
+                     o.arith, h->nsm, st);
+    launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
+    // exact nnz(C): rows that overflowed their slot can make it larger than the slot total
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        goto done;
+    }
+    if (hc.nnz > INT_MAX) {
+        rc = HSMU_ERR_OVERFLOW;
+        goto done;
+    }
+    CK(palloc(&ccol, (size_t)hc.nnz, st));
+    CK(palloc(&cval, (size_t)hc.nnz, st));
+    launch_compact(M, soff, crp, flag, scol, sval, ccol, cval, h->nsm, st);
+    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag}, win, win_cap, ctl,
+                     o.arith, h->nsm, st);
+    if (stats) cudaEventRecord(h->ev[4], st);
+    launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, flag, ctl, o.arith, h->nsm, st);
+    CK(cudaGetLastError());
+    if (stats) cudaEventRecord(h->ev[5], st);
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        goto done;
+    }
+    if (hc.nnz > INT_MAX) {
+        rc = HSMU_ERR_OVERFLOW;
+        goto done;
+    }
+    C->M = M;
+    C->N = B->N;
+    C->nnz = (int32_t)hc.nnz;
+    C->owned = 1;
+    C->row_ptr = crp;
+    C->col = ccol;
+    C->val = cval;
+    crp = nullptr;
+    ccol = nullptr;
+    cval = nullptr;
+    if (stats) {
+        float t;
+        stats->products = hc.products;
+        stats->nnz_c = hc.nnz;
+        stats->ntiles_b = hc.ntiles;
+        stats->windows = hc.win_count;
+        stats->spec_capacity = spec_total;
+        stats->fallback_rows = hc.fallback;
+        cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
+        stats->ms_convert = t;
+        cudaEventElapsedTime(&t, h->ev[1], h->ev[2]);
+        stats->ms_symbolic = t;
+        cudaEventElapsedTime(&t, h->ev[2], h->ev[3]);
+        stats->ms_alloc = t;
+        cudaEventElapsedTime(&t, h->ev[3], h->ev[4]);
+        stats->ms_structure = t;
+        cudaEventElapsedTime(&t, h->ev[4], h->ev[5]);
+        stats->ms_numeric = t;
+        cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
+        stats->ms_total = t;
+        // tiles 5, bounds 1, features 1, capacity 1, scan 3, structure 3, scan 3, compact 1, redo 3, numeric 1
+        stats->launches = (o.validate ? 2 : 0) + 22;
+    }
+done:
+    pfree(ctl, st);
+    pfree(bt.tile_ptr, st);
+    pfree(bt.tile_col, st);
+    pfree(bt.mask, st);
+    pfree(bt.tile_off, st);
+    pfree(ri.prod, st);
+    pfree(ri.tmin, st);
+    pfree(ri.tmax, st);
+    pfree(ri.bins, st);
+    pfree(ri.cnnz, st);
+    pfree(scan_tmp, st);
+    pfree(feat, st);
+    pfree(cap, st);
+    pfree(soff, st);
+    pfree(flag, st);
+    pfree(scol, st);
+    pfree(sval, st);
+    pfree(win, st);
+    pfree(crp, st);
+    pfree(ccol, st);
+    pfree(cval, st);
+    if (rc != HSMU_OK) cudaStreamSynchronize(st);
+    return rc;
+}
+
+// exact nnz of every row of A*B through the symbolic pass (training labels)
+int row_nnz_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, int32_t *nnz_out, cudaStream_t st) {
+    if (!h || !csr_ok(A) || !csr_ok(B) || !nnz_out || A->N != B->M) return HSMU_ERR_INVALID;
+    const int M = A->M;
+    int rc = HSMU_OK;
+    Ctl *ctl = nullptr;
+    hsmu_btiles bt{};
+    RowInfo ri{};
+    DevCSR Ad = dev(A), Bd = dev(B);
+    DevTiles Btd{};
+    CK(palloc(&ctl, 1, st));
+    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    rc = build_tiles(h, B, &bt, ctl, 0, st, false);
+    if (rc) goto done;
+    Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
+    CK(palloc(&ri.prod, (size_t)M, st));
+    CK(palloc(&ri.tmin, (size_t)M, st));
+    CK(palloc(&ri.tmax, (size_t)M, st));
+    CK(palloc(&ri.bins, (size_t)M * NBIN, st));
+    ri.cnnz = nnz_out;
+    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
+    launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h->h_ctl->err) rc = err_from_dev(h->h_ctl->err);
+done:
+    pfree(ctl, st);
+    pfree(bt.tile_ptr, st);
+    pfree(bt.tile_col, st);
+    pfree(bt.mask, st);
+    pfree(bt.tile_off, st);
+    pfree(ri.prod, st);
+    pfree(ri.tmin, st);
+    pfree(ri.tmax, st);
+    pfree(ri.bins, st);
     if (rc != HSMU_OK) cudaStreamSynchronize(st);
     return rc;
 }
@@ -354,6 +571,15 @@ int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, const
                       const hsmu_opts *opts, void *stream, hsmu_stats *stats) {
     if (!Bt) return HSMU_ERR_INVALID;
     return spgemm_impl(h, A, B, Bt, C, opts, static_cast<cudaStream_t>(stream), stats);
+}
+
+int hsmu_spgemm_learned(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
+                        const hsmu_opts *opts, void *stream, hsmu_stats *stats) {
+    return spgemm_learned_impl(h, A, B, C, model, opts, static_cast<cudaStream_t>(stream), stats);
+}
+
+int hsmu_row_nnz(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, int32_t *nnz, void *stream) {
+    return row_nnz_impl(h, A, B, nnz, static_cast<cudaStream_t>(stream));
 }
 
 int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream) {

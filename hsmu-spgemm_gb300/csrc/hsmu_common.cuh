@@ -53,9 +53,10 @@ enum DevErr : int {
 
 struct Window {
     int row;   // C row
-    int s0;    // absolute index of the first slot (C entry) of the window
+    int s0;    // first slot of the window, relative to the row's first entry
     int cnt;   // number of slots
     int t0;    // tile id of the first slot's column
+    int redo;  // 1 when emitted by the redo pass of the learned path
 };
 
 struct Ctl {
@@ -67,7 +68,8 @@ struct Ctl {
     int win_next;                    // dynamic work counter of the numeric pass
     int err;
     int ntiles;                      // B tiles (after the B conversion scan)
-    int pad[2];
+    int fallback;                    // learned path: rows that did not fit their slot
+    int pad;
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -24,6 +24,19 @@ struct DevTiles {
     const int *off;                  // [T]
 };
 
+// where the structure pass puts each row (see k_structure.cu)
+enum OutMode : int { OUT_PLAIN = 0, OUT_SPEC = 1, OUT_REDO = 2 };
+enum RowFlag : unsigned char { ROW_NONE = 0, ROW_VALUES = 1, ROW_COLUMNS = 2, ROW_OVERFLOW = 3 };
+struct RowOut {
+    int mode;
+    const int *crp;         // PLAIN / REDO: final row pointers
+    const long long *soff;  // SPEC: speculative slot offsets [M+1]
+    int *ccol;              // destination columns
+    double *cval;           // destination values
+    int *cnnz;              // SPEC: exact nnz found per row
+    unsigned char *flag;    // SPEC: written; REDO: rows flagged ROW_OVERFLOW are redone
+};
+
 // per-row data of A produced by the bounds kernel
 struct RowInfo {
     long long *prod;   // intermediate products of the row
@@ -46,6 +59,15 @@ void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo
 // sets DERR_OVERFLOW if the total exceeds INT32_MAX.  tmp must hold scan_tmp_ints(n) ints.
 size_t scan_tmp_ints(int n);
 void launch_scan(const int *in, int *out, int n, long long *total64, int *tmp, Ctl *ctl, cudaStream_t st);
+// same with int64 output (no overflow limit)
+void launch_scan64(const int *in, long long *out, int n, long long *total64, int *tmp, cudaStream_t st);
+
+// learned.cu
+void launch_features(const DevCSR &A, const DevCSR &B, float4 *feat, long long *prod_out, int nsm, cudaStream_t st);
+void launch_capacity(const float *params, const float4 *feat, const long long *prod, int M, int N, float margin,
+                     int *cap, int nsm, cudaStream_t st);
+void launch_compact(int M, const long long *soff, const int *crp, const unsigned char *flag, const int *scol,
+                    const double *sval, int *ccol, double *cval, int nsm, cudaStream_t st);
 
 // k_symbolic.cu
 void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
@@ -53,12 +75,14 @@ void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo 
 
 // k_structure.cu
 // writes C's columns and numeric windows; rows that fit one warp also get their values
-void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol,
-                      double *cval, Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
+void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
+                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
 
 // k_numeric.cu
+// flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped
 void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, const int *ccol, double *cval,
-                    const Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
+                    const Window *win, long long win_cap, const unsigned char *flag, Ctl *ctl, int arith, int nsm,
+                    cudaStream_t st);
 
 int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st);
 

@@ -43,21 +43,22 @@ __device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__r
     return n;
 }
 
-// fills C's columns and values of the row at out_col/out_val (nnz entries
-// expected); returns false on an inconsistency (count mismatch / overflow).
+// Fills the row's sorted columns and values at out_col/out_val and returns
+// its nnz; returns -1 on an inconsistency (more than TINY_MAX products, or
+// more than `cap` distinct columns).
 template <bool NC = true, class MulFn>
-__device__ __forceinline__ bool tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
-                                              const double *__restrict__ aval, const int *__restrict__ brp,
-                                              const int *__restrict__ bcol, const double *__restrict__ bval,
-                                              int *cols, double *acc, int stride, int nnz, int *__restrict__ out_col,
-                                              double *__restrict__ out_val, MulFn mul) {
+__device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
+                                             const double *__restrict__ aval, const int *__restrict__ brp,
+                                             const int *__restrict__ bcol, const double *__restrict__ bval,
+                                             int *cols, double *acc, int stride, int cap, int *__restrict__ out_col,
+                                             double *__restrict__ out_val, MulFn mul) {
     int n = 0, seen = 0;
     for (int p = a_lo; p < a_hi; p++) {
         const int k = ldx<NC>(acol + p);
         const double a = ldx<NC>(aval + p);
         const int qe = ldx<NC>(brp + k + 1);
         for (int q = ldx<NC>(brp + k); q < qe; q++) {
-            if (++seen > TINY_MAX) return false;
+            if (++seen > TINY_MAX) return -1;
             const int j = ldx<NC>(bcol + q);
             const double pr = mul(a, ldx<NC>(bval + q));
             int pos = n;
@@ -75,12 +76,12 @@ __device__ __forceinline__ bool tiny_row_fill(int a_lo, int a_hi, const int *__r
             n++;
         }
     }
-    if (n != nnz) return false;
+    if (n > cap) return -1;
     for (int t = 0; t < n; t++) {
         out_col[t] = cols[t * stride];
         out_val[t] = acc[t * stride];
     }
-    return true;
+    return n;
 }
 
 }  // namespace hsmu

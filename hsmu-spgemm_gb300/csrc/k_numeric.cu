@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             const double *__restrict__ bval,
                                                             const int *__restrict__ crp, const int *__restrict__ ccol,
                                                             double *__restrict__ cval, const Window *__restrict__ win,
-                                                            int win_cap, Ctl *ctl) {
+                                                            int win_cap, const unsigned char *__restrict__ flag,
+                                                            Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
@@ -75,8 +76,14 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
         const int wend = min(nwin, (g + 1) * GW);
         for (int wi = g * GW; wi < wend; wi++) {
             const Window W = win[wi];
-            const int row = W.row, s0 = W.s0, cnt = W.cnt, t0 = W.t0;
-            if (cnt <= 0 || cnt > WIN_CAP) {
+            const int row = W.row, cnt = W.cnt, t0 = W.t0;
+            if (flag && flag[row] == ROW_OVERFLOW && !W.redo) {  // stale: the redo pass emitted fresh windows
+                prev_row = -1;
+                continue;
+            }
+            const int row_lo = crp[row], row_hi = crp[row + 1];
+            const int s0 = row_lo + W.s0;  // windows carry row-relative offsets
+            if (cnt <= 0 || cnt > WIN_CAP || W.s0 < 0 || s0 + cnt > row_hi) {
                 bad = true;
                 prev_row = -1;
                 continue;
@@ -88,7 +95,6 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 prev_row = -1;
                 continue;
             }
-            const int row_lo = crp[row], row_hi = crp[row + 1];
             const int a_lo = arp[row], a_hi = arp[row + 1];
             const bool first = s0 == row_lo;
             const bool last = s0 + cnt == row_hi;
@@ -180,10 +186,11 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
 }
 
 void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, const int *ccol, double *cval,
-                    const Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+                    const Window *win, long long win_cap, const unsigned char *flag, Ctl *ctl, int arith, int nsm,
+                    cudaStream_t st) {
     auto k = arith == 2 ? k_numeric<true> : k_numeric<false>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
-        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, ctl);
+        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, ctl);
 }
 
 int configure_numeric() {

@@ -179,6 +179,36 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_out(const int *__restrict__ in,
     }
 }
 
+__global__ void __launch_bounds__(SCAN_T) k_scan_out64(const int *__restrict__ in, long long *__restrict__ out, int n,
+                                                       const long long *__restrict__ boff,
+                                                       const long long *total64) {
+    __shared__ long long s_warp[SCAN_T / 32 + 1];
+    const long long base = (long long)blockIdx.x * SCAN_ITEMS + threadIdx.x * SCAN_IPT;
+    int vals[SCAN_IPT];
+    long long v = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; j++) {
+        vals[j] = base + j < n ? in[base + j] : 0;
+        v += vals[j];
+    }
+    long long tot;
+    long long ex = block_excl_scan(v, s_warp, tot) + boff[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < SCAN_IPT; j++) {
+        if (base + j < n) out[base + j] = ex;
+        ex += vals[j];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total64;
+}
+
+void launch_scan64(const int *in, long long *out, int n, long long *total64, int *tmp, cudaStream_t st) {
+    const int nb = n > 0 ? (n + SCAN_ITEMS - 1) / SCAN_ITEMS : 1;
+    long long *bsum = reinterpret_cast<long long *>(tmp);
+    k_scan_sums<<<nb, SCAN_T, 0, st>>>(in, n, bsum);
+    k_scan_top<<<1, SCAN_T, 0, st>>>(bsum, nb, total64);
+    k_scan_out64<<<nb, SCAN_T, 0, st>>>(in, out, n, bsum, total64);
+}
+
 size_t scan_tmp_ints(int n) {
     const int nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
     return (size_t)(nb > 0 ? nb : 1) * 2 + 2;

@@ -22,12 +22,26 @@
 // slot lookup of the value phase (slot = base[t] + popc(mask[t] below j)),
 // so the products are accumulated right away and the values written with no
 // window, no second walk over A and no re-read of C's columns.
+//
+// Output modes (RowOut): PLAIN writes every row at its final place (exact
+// counts came from the symbolic pass); SPEC (learned scheduler) writes every
+// row into a speculative slot sized by the predicted nnz, records the exact
+// count it finds and flags rows that did not fit; REDO runs PLAIN on the
+// flagged rows once the exact counts have been scanned.  Window offsets are
+// row-relative so they stay valid whichever buffer the columns were written to.
 #include "hsmu_block.cuh"
 #include "hsmu_kernels.h"
 #include "hsmu_products.cuh"
 #include "hsmu_rowops.cuh"
 
 namespace hsmu {
+
+__device__ __forceinline__ long long out_base(const RowOut &o, int i) {
+    return o.mode == OUT_SPEC ? o.soff[i] : (long long)o.crp[i];
+}
+__device__ __forceinline__ int out_limit(const RowOut &o, int i) {
+    return o.mode == OUT_SPEC ? (int)(o.soff[i + 1] - o.soff[i]) : o.crp[i + 1] - o.crp[i];
+}
 
 constexpr int SDS_WARPS = 4;
 constexpr int SDS_CTAS_PER_SM = 5;
@@ -47,20 +61,22 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
     k_struct_ds(int M, const int *__restrict__ arp, const int *__restrict__ acol, const double *__restrict__ aval,
                 const int *__restrict__ brp, const int *__restrict__ bcol, const double *__restrict__ bval,
                 const int *__restrict__ tptr, const int *__restrict__ tcol,
-                const unsigned long long *__restrict__ tmask, RowInfo ri, const int *__restrict__ crp,
-                int *__restrict__ ccol, double *__restrict__ cval, Window *__restrict__ win, long long win_cap,
-                Ctl *ctl) {
+                const unsigned long long *__restrict__ tmask, RowInfo ri, RowOut out, Window *__restrict__ win,
+                long long win_cap, Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     SdsSmem &S = reinterpret_cast<SdsSmem *>(s_dyn)[w];
     const int n = ctl->bin_count[BIN_DS];
     const int *rows = ri.bins + (size_t)BIN_DS * M;
+    int *__restrict__ ccol = out.ccol;
+    double *__restrict__ cval = out.cval;
     for (int r = blockIdx.x * SDS_WARPS + w; r < n; r += gridDim.x * SDS_WARPS) {
         const int i = rows[r];
+        if (out.mode == OUT_REDO && out.flag[i] != ROW_OVERFLOW) continue;
         const int t0 = ri.tmin[i];
         const int span = ri.tmax[i] - t0 + 1;
-        const int rowbase = crp[i];
-        const int nnz = crp[i + 1] - rowbase;
+        const long long rowbase = out_base(out, i);
+        const int limit = out_limit(out, i);
         for (int t = lane; t < span; t += WARP) S.msk[t] = 0ull;
         __syncwarp();
         bool bad = false;
@@ -70,7 +86,13 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             else bad = true;
         });
         if (__any_sync(FULL, bad)) {
-            if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
+            if (lane == 0) {
+                set_err(&ctl->err, DERR_INTERNAL);
+                if (out.mode == OUT_SPEC) {
+                    out.cnnz[i] = 0;
+                    out.flag[i] = ROW_OVERFLOW;
+                }
+            }
             __syncwarp();
             continue;
         }
@@ -81,7 +103,18 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
         for (int t = lo; t < hi; t++) sum += popc64(S.msk[t]);
         const int incl = warp_incl_scan(sum);
         const int total = __shfl_sync(FULL, incl, WARP - 1);
-        if (total != nnz) {
+        const int nnz = total;
+        if (out.mode == OUT_SPEC) {
+            if (lane == 0) {
+                out.cnnz[i] = total;
+                out.flag[i] = total > limit ? ROW_OVERFLOW : (total <= FUSE_CAP ? ROW_VALUES : ROW_COLUMNS);
+                if (total > limit) atomicAdd(&ctl->fallback, 1);
+            }
+            if (total > limit) {
+                __syncwarp();
+                continue;
+            }
+        } else if (total != limit) {
             if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
             __syncwarp();
             continue;
@@ -102,7 +135,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             for (int t = lo; t < hi; t++) {
                 unsigned long long m = S.msk[t];
                 if (m) {
-                    int pos = rowbase + S.base[t];
+                    long long pos = rowbase + S.base[t];
                     const int cb = (t0 + t) << 6;
                     while (m) {
                         ccol[pos++] = cb + (__ffsll((long long)m) - 1);
@@ -168,13 +201,13 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             for (int j = lane; j < nwin; j += WARP) {
                 const int s0 = S.wl[j];
                 const int e = (j + 1 < nwin) ? S.wl[j + 1] : total;
-                win[wbase + j] = Window{i, rowbase + s0, e - s0, t0 + S.wt[j]};
+                win[wbase + j] = Window{i, s0, e - s0, t0 + S.wt[j], out.mode == OUT_REDO};
             }
         }
         for (int t = lo; t < hi; t++) {
             unsigned long long m = S.msk[t];
             if (m) {
-                int pos = rowbase + S.base[t];
+                long long pos = rowbase + S.base[t];
                 const int cb = (t0 + t) << 6;
                 while (m) {
                     ccol[pos++] = cb + (__ffsll((long long)m) - 1);
@@ -210,8 +243,8 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                                                          const int *__restrict__ tptr,
                                                          const int *__restrict__ tcol,
                                                          const unsigned long long *__restrict__ tmask, RowInfo ri,
-                                                         const int *__restrict__ crp, int *__restrict__ ccol,
-                                                         Window *__restrict__ win, long long win_cap, Ctl *ctl) {
+                                                         RowOut out, Window *__restrict__ win, long long win_cap,
+                                                         Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     SlSmem &S = *reinterpret_cast<SlSmem *>(s_dyn);
     __shared__ int s_tmp[SL_THREADS / 32 + 1];
@@ -221,12 +254,14 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
     const int w = threadIdx.x >> 5;
     const int n = ctl->bin_count[BIN_L];
     const int *rows = ri.bins + (size_t)BIN_L * M;
+    int *__restrict__ ccol = out.ccol;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
         const int i = rows[r];
+        if (out.mode == OUT_REDO && out.flag[i] != ROW_OVERFLOW) continue;
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
         const int a_lo = arp[i], a_hi = arp[i + 1];
-        const int rowbase = crp[i];
-        const int nnz = crp[i + 1] - rowbase;
+        const long long rowbase = out_base(out, i);
+        const int nnz = out_limit(out, i);  // exact (PLAIN/REDO) or capacity (SPEC)
         const bool one_chunk = (tmax - tmin + 1) <= DCH_STRUCT;
         int run_row = 0, tiles_row = 0;
         for (int c0 = tmin; c0 <= tmax; c0 += DCH_STRUCT) {
@@ -298,22 +333,27 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                         kk = key;
                     }
             }
-            if (threadIdx.x == 0) s_wbase = (nwin <= SL_WL) ? atomicAdd(&ctl->win_count, nwin) : -1;
+            if (threadIdx.x == 0)
+                s_wbase = (nwin <= SL_WL && !(out.mode == OUT_SPEC && run_row + chunk_total > nnz))
+                              ? atomicAdd(&ctl->win_count, nwin)
+                              : -1;
             __syncthreads();
             const int wbase = s_wbase;
             const int chunk_end = run_row + chunk_total;
-            if (wbase < 0 || (long long)wbase + nwin > win_cap || chunk_end > nnz) {
+            if (chunk_end > nnz && out.mode == OUT_SPEC) {
+                // does not fit its speculative slot: keep counting, write nothing more
+            } else if (wbase < 0 || (long long)wbase + nwin > win_cap || chunk_end > nnz) {
                 if (threadIdx.x == 0) set_err(&ctl->err, wbase < 0 || chunk_end <= nnz ? DERR_CAPACITY : DERR_INTERNAL);
             } else {
                 for (int j = threadIdx.x; j < nwin; j += SL_THREADS) {
                     const int s0 = S.wl[j];
                     const int e = (j + 1 < nwin) ? S.wl[j + 1] : chunk_end;
-                    win[wbase + j] = Window{i, rowbase + s0, e - s0, c0 + S.wt[j]};
+                    win[wbase + j] = Window{i, s0, e - s0, c0 + S.wt[j], out.mode == OUT_REDO};
                 }
                 for (int t = lo; t < hi; t++) {
                     unsigned long long m = S.msk[t];
                     if (m) {
-                        int p = rowbase + S.base[t];
+                        long long p = rowbase + S.base[t];
                         const int cb = (c0 + t) << 6;
                         while (m) {
                             ccol[p++] = cb + (__ffsll((long long)m) - 1);
@@ -326,7 +366,15 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             tiles_row += chunk_tiles;
             __syncthreads();
         }
-        if (threadIdx.x == 0 && run_row != nnz) set_err(&ctl->err, DERR_INTERNAL);
+        if (threadIdx.x == 0) {
+            if (out.mode == OUT_SPEC) {
+                out.cnnz[i] = run_row;
+                out.flag[i] = run_row > nnz ? ROW_OVERFLOW : ROW_COLUMNS;
+                if (run_row > nnz) atomicAdd(&ctl->fallback, 1);
+            } else if (run_row != nnz) {
+                set_err(&ctl->err, DERR_INTERNAL);
+            }
+        }
     }
 }
 
@@ -340,8 +388,7 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
                                                              const int *__restrict__ brp,
                                                              const int *__restrict__ bcol,
                                                              const double *__restrict__ bval, RowInfo ri,
-                                                             const int *__restrict__ crp, int *__restrict__ ccol,
-                                                             double *__restrict__ cval, Ctl *ctl) {
+                                                             RowOut out, Ctl *ctl) {
     __shared__ int s_cols[TINY_MAX * TINYF_THREADS];
     __shared__ double s_acc[TINY_MAX * TINYF_THREADS];
     const int n = ctl->bin_count[BIN_TINY];
@@ -349,23 +396,31 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
     bool bad = false;
     for (int r = blockIdx.x * TINYF_THREADS + threadIdx.x; r < n; r += gridDim.x * TINYF_THREADS) {
         const int i = rows[r];
-        const int c0 = crp[i];
-        if (!tiny_row_fill(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, s_cols + threadIdx.x,
-                           s_acc + threadIdx.x, TINYF_THREADS, crp[i + 1] - c0, ccol + c0, cval + c0,
-                           [](double x, double y) { return prod_mul<INT_MUL>(x, y); }))
+        if (out.mode == OUT_REDO && out.flag[i] != ROW_OVERFLOW) continue;
+        const long long c0 = out_base(out, i);
+        const int lim = out_limit(out, i);
+        const int got = tiny_row_fill(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, s_cols + threadIdx.x,
+                                      s_acc + threadIdx.x, TINYF_THREADS, lim, out.ccol + c0, out.cval + c0,
+                                      [](double x, double y) { return prod_mul<INT_MUL>(x, y); });
+        if (out.mode == OUT_SPEC) {
+            out.cnnz[i] = got < 0 ? 0 : got;
+            out.flag[i] = got < 0 ? ROW_OVERFLOW : ROW_VALUES;
+            if (got < 0) bad = true;  // tiny rows get a capacity that always fits
+        } else if (got != lim) {
             bad = true;
+        }
     }
     if (bad) set_err(&ctl->err, DERR_INTERNAL);
 }
 
-void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, const int *crp, int *ccol,
-                      double *cval, Window *win, long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
+                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
     auto kt = arith == 2 ? k_fill_tiny<true> : k_fill_tiny<false>;
-    kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, crp, ccol, cval, ctl);
+    kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, out, ctl);
     auto kds = arith == 2 ? k_struct_ds<true> : k_struct_ds<false>;
     kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
-        A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol, cval, win, win_cap, ctl);
-    k_struct_l<<<nsm * 2, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, crp, ccol,
+        A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
+    k_struct_l<<<nsm * 2, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
                                                             win, win_cap, ctl);
 }
 

@@ -38,7 +38,9 @@ EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_hand
            "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul", "hsmu_btiles_build_noalloc",
            "hsmu_batch_create", "hsmu_batch_execute", "hsmu_batch_graph_launch", "hsmu_batch_status",
            "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
-           "hsmu_gen_poisson7", "hsmu_gen_aggregation"]
+           "hsmu_gen_poisson7", "hsmu_gen_aggregation", "hsmu_spgemm_learned", "hsmu_row_features",
+           "hsmu_row_nnz", "hsmu_mlp_forward", "hsmu_mlp_grad", "hsmu_mlp_adam"]
+MLP_FLOATS = 1259
 
 
 class HsmuError(RuntimeError):
@@ -65,13 +67,18 @@ class c_opts(ctypes.Structure):
                 ("window_cap", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
+class c_mlp(ctypes.Structure):
+    _fields_ = [("params", ctypes.c_void_p), ("margin", ctypes.c_float), ("reserved", ctypes.c_int32)]
+
+
 class c_stats(ctypes.Structure):
     _fields_ = [("products", ctypes.c_uint64), ("nnz_c", ctypes.c_int64),
                 ("ntiles_b", ctypes.c_int64), ("windows", ctypes.c_int64),
                 ("ms_convert", ctypes.c_float), ("ms_symbolic", ctypes.c_float),
                 ("ms_alloc", ctypes.c_float), ("ms_structure", ctypes.c_float),
                 ("ms_numeric", ctypes.c_float), ("ms_total", ctypes.c_float),
-                ("launches", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("launches", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("spec_capacity", ctypes.c_int64), ("fallback_rows", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -118,6 +125,13 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_batch_destroy.argtypes = [P]
     L.hsmu_gen_poisson7.argtypes = [ctypes.c_int, ctypes.POINTER(c_csr), P]
     L.hsmu_gen_aggregation.argtypes = [ctypes.c_int, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), P]
+    L.hsmu_spgemm_learned.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
+                                      ctypes.POINTER(c_mlp), ctypes.POINTER(c_opts), P, ctypes.POINTER(c_stats)]
+    L.hsmu_row_features.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), P, P, P]
+    L.hsmu_row_nnz.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), P, P]
+    L.hsmu_mlp_forward.argtypes = [P, P, ctypes.c_int, P, P]
+    L.hsmu_mlp_grad.argtypes = [P, P, P, ctypes.c_int, P, P, P]
+    L.hsmu_mlp_adam.argtypes = [P, P, P, P, ctypes.c_float, ctypes.c_float, ctypes.c_int, P]
     L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
     _lib = L
     return L
@@ -283,6 +297,39 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+    def spgemm_learned(self, A: DeviceCSR, B: DeviceCSR, params, margin: float, *, arith: int = 0,
+                       validate: bool = False, stream=None, stats: bool = False) -> DeviceCSR:
+        """C = A * B with predicted row slots (hsmu_spgemm_learned); params: device float tensor."""
+        L = load_library()
+        C = c_csr()
+        o = c_opts(int(validate), int(arith), 0)
+        m = c_mlp(params.data_ptr(), float(margin), 0)
+        st = c_stats()
+        rc = L.hsmu_spgemm_learned(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc), ctypes.byref(C),
+                                   ctypes.byref(m), ctypes.byref(o), _stream_ptr(stream),
+                                   ctypes.byref(st) if stats else None)
+        _check(rc, "hsmu_spgemm_learned")
+        self.last_stats = st.as_dict() if stats else None
+        return DeviceCSR(C)
+
+    def row_features(self, A: DeviceCSR, B: DeviceCSR, stream=None):
+        """(features [M,4] float32, products [M] int64) as device tensors."""
+        torch = _torch()
+        f = torch.empty((A.M, 4), dtype=torch.float32, device="cuda")
+        p = torch.empty(A.M, dtype=torch.int64, device="cuda")
+        _check(load_library().hsmu_row_features(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc),
+                                                f.data_ptr(), p.data_ptr(), _stream_ptr(stream)),
+               "hsmu_row_features")
+        return f, p
+
+    def row_nnz(self, A: DeviceCSR, B: DeviceCSR, stream=None):
+        """exact nnz of every row of A*B (device int32 tensor) from the symbolic pass."""
+        torch = _torch()
+        n = torch.empty(A.M + 1, dtype=torch.int32, device="cuda")
+        _check(load_library().hsmu_row_nnz(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc), n.data_ptr(),
+                                           _stream_ptr(stream)), "hsmu_row_nnz")
+        return n[:A.M]
 
     def spgemm(self, A: DeviceCSR, B: DeviceCSR, *, validate: bool = False, arith: int = 0,
                tiles: BTiles | None = None, stream=None, stats: bool = False) -> DeviceCSR:

@@ -102,6 +102,8 @@ typedef struct hsmu_stats {
     float ms_total;
     int32_t launches;        /* kernels this call launched */
     int32_t reserved;
+    int64_t spec_capacity;   /* learned path: entries of the speculative slots */
+    int64_t fallback_rows;   /* learned path: rows that exceeded their slot and were redone */
 } hsmu_stats;
 
 typedef struct hsmu_handle_s *hsmu_handle;
@@ -156,6 +158,37 @@ int hsmu_csr_free(hsmu_csr *C);
  * row_ptr[M+1], col[nnz], val[nnz].  Stream-ordered; synchronizes `stream`
  * before returning. */
 int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream);
+
+/* ---- Learned row scheduler ----------------------------------------------
+ * hsmu_spgemm_learned computes the same C as hsmu_spgemm (bit for bit) but
+ * replaces the exact symbolic count pass with a prediction: a 3-layer FP32
+ * MLP (4 -> 32 -> 32 -> 1) maps each row's features (log2(1+x) of A-row nnz,
+ * intermediate products, longest referenced B row, column span) to log2 of
+ * its nnz; each row gets a slot of min(products, N, 2^(prediction + margin))
+ * entries, the structure pass writes into the slot and finds the exact count,
+ * rows that overflow are redone after the scan.  params: HSMU_MLP_FLOATS
+ * device floats (W1[32][4] b1[32] W2[32][32] b2[32] W3[32] b3, then mu[4]
+ * sd[4] ymu ysd).  No counterpart in the reference.
+ * hsmu_row_features / hsmu_row_nnz produce training data (features, and
+ * labels from the engine's own exact symbolic pass); hsmu_mlp_forward /
+ * hsmu_mlp_grad / hsmu_mlp_adam are the inference and training kernels
+ * (grad adds to `grad` and `loss`; adam applies grad * scale). */
+#define HSMU_MLP_FLOATS 1259
+typedef struct hsmu_mlp {
+    const float *params;
+    float margin;
+    int32_t reserved;
+} hsmu_mlp;
+int hsmu_spgemm_learned(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
+                        const hsmu_opts *opts, void *stream, hsmu_stats *stats);
+int hsmu_row_features(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, float *feat, int64_t *products,
+                      void *stream);
+int hsmu_row_nnz(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, int32_t *nnz, void *stream);
+int hsmu_mlp_forward(const float *params, const float *feat, int n, float *out, void *stream);
+int hsmu_mlp_grad(const float *params, const float *feat, const float *target, int n, float *grad, float *loss,
+                  void *stream);
+int hsmu_mlp_adam(float *params, const float *grad, float *m, float *v, float lr, float scale, int step,
+                  void *stream);
 
 /* ---- Batched persistent engine ------------------------------------------
  * Many independent products in ONE cooperative persistent launch, with no

@@ -1,0 +1,146 @@
+"""Learned row scheduler: FP32 kernels against the FP64 restatement, training,
+and the speculative SpGEMM path against the plain engine (bit for bit)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from hsmu_gb import gen
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_params(seed=0):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(mlp_ref.NTOTAL, np.float32)
+    p[:mlp_ref.NPARAM] = rng.normal(0, 0.3, mlp_ref.NPARAM)
+    p[mlp_ref.O_MU:mlp_ref.O_SD] = [3.0, 8.0, 5.0, 12.0]
+    p[mlp_ref.O_SD:mlp_ref.O_YMU] = [1.5, 3.0, 2.0, 4.0]
+    p[mlp_ref.O_YMU] = 7.0
+    p[mlp_ref.O_YSD] = 2.5
+    return p
+
+
+def rand_data(n, seed=1):
+    rng = np.random.default_rng(seed)
+    X = np.abs(rng.normal([3, 8, 5, 12], [1.5, 3, 2, 4], size=(n, 4))).astype(np.float32)
+    y = (0.6 * X[:, 1] + 0.2 * X[:, 3] + rng.normal(0, 0.3, n)).astype(np.float32)
+    return X, y
+
+
+def test_mlp_forward_matches_fp64():
+    from hsmu_gb import learned
+
+    p = rand_params()
+    X, _ = rand_data(5000)
+    got = learned.predict(p, X)
+    want = mlp_ref.forward(p.astype(np.float64), X)
+    assert np.max(np.abs(got - want)) <= 1e-4 * (1 + np.max(np.abs(want)))
+
+
+def test_mlp_gradient_matches_fp64():
+    import torch
+
+    import hsmu_gb
+
+    L = hsmu_gb.load_library()
+    p = rand_params(2)
+    X, y = rand_data(3000, 3)
+    g = torch.zeros(mlp_ref.NPARAM, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    pd, Xd, yd = (torch.from_numpy(a).cuda() for a in (p, X, y))
+    assert L.hsmu_mlp_grad(pd.data_ptr(), Xd.data_ptr(), yd.data_ptr(), X.shape[0], g.data_ptr(),
+                           loss.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    want_loss, want = mlp_ref.loss_and_grad(p.astype(np.float64), X, y)
+    got = g.cpu().numpy().astype(np.float64)
+    assert abs(loss.item() - want_loss) <= 1e-4 * want_loss
+    err = np.abs(got - want) / (np.abs(want) + 1e-3 * np.max(np.abs(want)))
+    assert err.max() <= 1e-3, (err.argmax(), got[err.argmax()], want[err.argmax()])
+
+
+def test_training_reduces_loss(engine):
+    from hsmu_gb import learned
+
+    X, y = learned.collect(engine, nmat=18, rows_per_matrix=96, seed=5, workers=1)
+    assert X.shape[0] > 200 and np.all(np.isfinite(X))
+    params, hist = learned.train(X, y, epochs=12, batch=512, lr=3e-3, seed=1)
+    assert hist[-1] < 0.5 * hist[0]
+    pred = learned.predict(params, X)
+    assert np.mean(np.abs(pred - y)) < 1.0  # within a factor of 2 of nnz on average
+
+
+def model_for_tests(engine):
+    from hsmu_gb import learned
+
+    if os.path.exists(learned.DEFAULT_MODEL):
+        p, margin, _ = learned.load()
+        return p, margin
+    X, y = learned.collect(engine, nmat=24, rows_per_matrix=128, seed=7, workers=1)
+    p, _ = learned.train(X, y, epochs=15, batch=512, lr=3e-3)
+    return p, learned.choose_margin(p, X, y, 0.99)
+
+
+def run_both(engine, A, B, params, margin):
+    import torch
+
+    import hsmu_gb
+
+    dA = hsmu_gb.DeviceCSR.from_host(A)
+    dB = dA if B is A else hsmu_gb.DeviceCSR.from_host(B)
+    P = engine.spgemm(dA, dB).to_host()
+    pt = torch.from_numpy(np.ascontiguousarray(params, np.float32)).cuda()
+    Cd = engine.spgemm_learned(dA, dB, pt, margin, stats=True)
+    st = engine.last_stats
+    return P, Cd.to_host(), st
+
+
+@pytest.mark.parametrize("name", ["lap", "st27", "rmat12", "rmat13T", "rect", "wide"])
+def test_learned_identical_to_plain(engine, name):
+    p, margin = model_for_tests(engine)
+    if name == "lap":
+        A = B = gen.laplacian2d(64, seed=0)
+    elif name == "st27":
+        A = B = gen.stencil27(10, 3, seed=1)
+    elif name == "rmat12":
+        A = B = gen.rmat(12, 16, seed=2, lo=-1.0, hi=1.0)
+    elif name == "rmat13T":
+        A = gen.rmat(13, 16, seed=2)
+        B = gen.transpose(A)
+    elif name == "rect":
+        A = gen.poisson_random(3000, 12, seed=5, ncols=50000)
+        B = gen.poisson_random(50000, 6, seed=6, ncols=70000)
+    else:
+        A = gen.poisson_random(400, 40, seed=7, ncols=2000)
+        B = gen.poisson_random(2000, 60, seed=8, ncols=1_200_000)
+    P, C, st = run_both(engine, A, B, p, margin)
+    np.testing.assert_array_equal(C.row_ptr, P.row_ptr)
+    np.testing.assert_array_equal(C.col, P.col)
+    assert np.array_equal(C.val.view(np.int64), P.val.view(np.int64))
+    assert st["nnz_c"] == P.nnz
+    if st["spec_capacity"] < P.nnz:  # only possible when some rows overflowed their slots
+        assert st["fallback_rows"] > 0
+
+
+def test_learned_all_rows_fall_back(engine):
+    # a model that predicts nothing fits: every non-tiny row is redone, result unchanged
+    p, _ = model_for_tests(engine)
+    A = gen.rmat(12, 16, seed=4, lo=-1.0, hi=1.0)
+    P, C, st = run_both(engine, A, A, p, -40.0)
+    assert st["fallback_rows"] > 0
+    np.testing.assert_array_equal(C.col, P.col)
+    assert np.array_equal(C.val.view(np.int64), P.val.view(np.int64))
+    rp, col, val = oracle.spgemm(A, A)
+    assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
+def test_trained_model_sizes_slots_tighter_than_the_bound(engine):
+    # what the network gains: slot memory close to nnz(C), instead of the product-count bound
+    p, margin = model_for_tests(engine)
+    A = gen.stencil27(14, 3, seed=1)
+    P, C, st = run_both(engine, A, A, p, margin)
+    prods = gen.products(A, A)
+    assert st["spec_capacity"] < 0.25 * prods           # the bound would allocate `prods` entries
+    assert st["fallback_rows"] <= 0.05 * A.M
