@@ -56,6 +56,8 @@ WORKLOADS = {
     "laplacian2d_256_AA": "5-point Laplacian, 256^2 grid (n=65,536), C=A*A, uniform(-1,1), seed 0",
     "rmat18_AA": "R-MAT scale 18, edge factor 16, (0.57,0.19,0.19,0.05), merged, uniform(0,1), seed 2, C=A*A",
     "rmat18_AAt": "R-MAT scale 18, edge factor 16, merged, uniform(0,1), seed 2, C=A*A^T",
+    "rmat20_panels": "R-MAT scale 20, edge factor 16, merged, uniform(0,1), seed 3, C=A*A in row panels of at most "
+                     "1.9e9 products each (nnz(C) ~ 1e10 does not fit one int32 CSR); learned scheduler vs plain",
     "amg512_galerkin": "512 AMG Galerkin products P^T(A P): A 7-point Poisson on side^3 grids, side uniform "
                        "in [16,96] (seed 4), P 2x2x2 aggregation; batched persistent engine under a CUDA graph "
                        "vs 1,024 plain calls",
@@ -450,6 +452,72 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def run_learned_panels(args):
+    """Learned scheduler vs plain engine on R-MAT scale 20, processed in row panels."""
+    import numpy as np
+    import torch
+
+    import hsmu_gb
+    from hsmu_gb import gen, learned
+
+    A = gen.rmat(20, 16, seed=3)
+    blen = np.diff(A.row_ptr).astype(np.int64)
+    cs = np.concatenate(([0], np.cumsum(blen[A.col])))
+    rowprod = cs[A.row_ptr[1:]] - cs[A.row_ptr[:-1]]
+    cum = np.concatenate(([0], np.cumsum(rowprod)))
+    cuts = [0]
+    while cuts[-1] < A.M:  # panels of at most 1.9e9 products (so nnz(C) < 2^31)
+        nxt = int(np.searchsorted(cum, cum[cuts[-1]] + 1.9e9, side="right")) - 1
+        cuts.append(max(nxt, cuts[-1] + 1) if nxt < A.M else A.M)
+    eng = hsmu_gb.Engine()
+    dA = hsmu_gb.DeviceCSR.from_host(A)
+    params, margin, meta = learned.load()
+    pt = torch.from_numpy(params).cuda()
+
+    def panel(r0, r1):
+        c = hsmu_gb.c_csr(r1 - r0, A.N, A.nnz, 0, dA.desc.row_ptr + 4 * r0, dA.desc.col, dA.desc.val)
+        return hsmu_gb.DeviceCSR(c, keep=dA)
+
+    panels = [panel(cuts[k], cuts[k + 1]) for k in range(len(cuts) - 1)]
+    # warm-up on the first panel
+    eng.spgemm(panels[0], dA).free()
+    eng.spgemm_learned(panels[0], dA, pt, margin).free()
+    res = {"plain": [], "learned": []}
+    fallback = capacity = nnz_total = 0
+    for P in panels:
+        for mode in ("plain", "learned"):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mode == "plain":
+                C = eng.spgemm(P, dA, stats=True)
+            else:
+                C = eng.spgemm_learned(P, dA, pt, margin, stats=True)
+            torch.cuda.synchronize()
+            res[mode].append(time.perf_counter() - t0)
+            st = eng.last_stats
+            if mode == "learned":
+                fallback += st["fallback_rows"]
+                capacity += st["spec_capacity"]
+                nnz_total += st["nnz_c"]
+            C.free()
+    products = int(cum[-1])
+    tp, tl = sum(res["plain"]), sum(res["learned"])
+    line = {
+        "metric": METRIC, "value": round(2.0 * products / tl / 1e9, 3), "unit": "GFLOPS", "n_gpus": 1,
+        "steps": 1, "warmup": 1, "ms_per_step": round(tl * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-MAT scale 20)",
+        "config": {"workload": "rmat20_panels", "desc": WORKLOADS["rmat20_panels"], "n": A.M, "nnz_A": A.nnz,
+                   "products": products, "nnz_C": nnz_total, "panels": len(panels)},
+        "learned": {"ms": round(tl * 1e3, 3), "plain_ms": round(tp * 1e3, 3), "speedup_vs_plain": round(tp / tl, 3),
+                    "fallback_rows": fallback, "slot_entries": capacity,
+                    "slot_entries_over_nnz": round(capacity / max(1, nnz_total), 3),
+                    "product_bound_over_nnz": round(products / max(1, nnz_total), 3),
+                    "model": {k: v for k, v in meta.items() if k != "train_loss"}, "margin": margin},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,6 +530,8 @@ def main():
         run_reference(args)
     elif args.workload == "amg512_galerkin":
         run_batched(args)
+    elif args.workload == "rmat20_panels":
+        run_learned_panels(args)
     else:
         run_engine(args)
 

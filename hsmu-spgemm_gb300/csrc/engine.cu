@@ -228,7 +228,8 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
                          ctl, o.arith, h->nsm, st);
     if (stats) cudaEventRecord(h->ev[4], st);
     // 5b. values
-    if (hc.nnz > 0) launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, nullptr, ctl, o.arith, h->nsm, st);
+    if (hc.nnz > 0)
+        launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, ctl, o.arith, h->nsm, st);
     CK(cudaGetLastError());
     if (stats) cudaEventRecord(h->ev[5], st);
 
@@ -395,7 +396,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag}, win, win_cap, ctl,
                      o.arith, h->nsm, st);
     if (stats) cudaEventRecord(h->ev[4], st);
-    launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, flag, ctl, o.arith, h->nsm, st);
+    launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, flag, scol, soff, ctl, o.arith, h->nsm, st);
     CK(cudaGetLastError());
     if (stats) cudaEventRecord(h->ev[5], st);
     CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));

@@ -79,10 +79,12 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
                       long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
 
 // k_numeric.cu
-// flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped
-void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, const int *ccol, double *cval,
-                    const Window *win, long long win_cap, const unsigned char *flag, Ctl *ctl, int arith, int nsm,
-                    cudaStream_t st);
+// flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped;
+// scol/soff (nullable): speculative slots holding the columns of speculative-pass
+// windows, which the kernel copies to ccol
+void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, int *ccol, double *cval,
+                    const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
+                    const long long *soff, Ctl *ctl, int arith, int nsm, cudaStream_t st);
 
 int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st);
 

@@ -59,10 +59,11 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             const double *__restrict__ aval,
                                                             const int *__restrict__ brp, const int *__restrict__ bcol,
                                                             const double *__restrict__ bval,
-                                                            const int *__restrict__ crp, const int *__restrict__ ccol,
+                                                            const int *__restrict__ crp, int *__restrict__ ccol,
                                                             double *__restrict__ cval, const Window *__restrict__ win,
                                                             int win_cap, const unsigned char *__restrict__ flag,
-                                                            Ctl *ctl) {
+                                                            const int *__restrict__ scol,
+                                                            const long long *__restrict__ soff, Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
@@ -88,7 +89,11 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 prev_row = -1;
                 continue;
             }
-            const int c_lo = ccol[s0], c_hi = ccol[s0 + cnt - 1];
+            // columns of the window: in C, or (learned path, speculative pass) still in the row's
+            // slot -- then they are copied to C here while the table is built
+            const bool from_slot = scol != nullptr && !W.redo;
+            const int *__restrict__ src = from_slot ? scol + soff[row] + W.s0 : ccol + s0;
+            const int c_lo = src[0], c_hi = src[cnt - 1];
             const int span = (c_hi >> 6) - t0 + 1;
             if (span <= 0 || span > WIN_SPAN || (c_lo >> 6) != t0) {
                 bad = true;
@@ -117,7 +122,8 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 for (int sb = 0; sb < cnt; sb += WARP) {
                     const int s = sb + lane;
                     const bool v = s < cnt;
-                    const int c = v ? ccol[s0 + s] : 0;
+                    const int c = v ? src[s] : 0;
+                    if (v && from_slot) ccol[s0 + s] = c;
                     const int t = (c >> 6) - t0;
                     int tp = __shfl_up_sync(FULL, t, 1);
                     if (lane == 0) tp = prev_t;
@@ -185,12 +191,12 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
     if (__any_sync(FULL, bad) && lane == 0) set_err(&ctl->err, DERR_INTERNAL);
 }
 
-void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, const int *ccol, double *cval,
-                    const Window *win, long long win_cap, const unsigned char *flag, Ctl *ctl, int arith, int nsm,
-                    cudaStream_t st) {
+void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, int *ccol, double *cval,
+                    const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
+                    const long long *soff, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
     auto k = arith == 2 ? k_numeric<true> : k_numeric<false>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
-        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, ctl);
+        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, ctl);
 }
 
 int configure_numeric() {

@@ -261,7 +261,9 @@ __global__ void __launch_bounds__(256) k_capacity(const float *__restrict__ para
     }
 }
 
-// copy rows written into their speculative slots to their final place
+// copy rows fused in their speculative slots (columns and values, at most a
+// few hundred entries each) to their final place; the columns of wider rows
+// are copied by the value kernel, window by window
 __global__ void __launch_bounds__(256) k_compact(int M, const long long *__restrict__ soff,
                                                  const int *__restrict__ crp, const unsigned char *__restrict__ flag,
                                                  const int *__restrict__ scol, const double *__restrict__ sval,
@@ -269,13 +271,13 @@ __global__ void __launch_bounds__(256) k_compact(int M, const long long *__restr
     const int lane = lane_id();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < M; i += nw) {
-        const unsigned char f = flag[i];
-        if (f != ROW_VALUES && f != ROW_COLUMNS) continue;
+        if (flag[i] != ROW_VALUES) continue;
         const long long src = soff[i];
         const int dst = crp[i], n = crp[i + 1] - dst;
-        for (int q = lane; q < n; q += WARP) ccol[dst + q] = scol[src + q];
-        if (f == ROW_VALUES)
-            for (int q = lane; q < n; q += WARP) cval[dst + q] = sval[src + q];
+        for (int q = lane; q < n; q += WARP) {
+            ccol[dst + q] = scol[src + q];
+            cval[dst + q] = sval[src + q];
+        }
     }
 }
 
