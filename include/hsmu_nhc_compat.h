@@ -1,0 +1,272 @@
+/*
+ * hsmu_nhc_compat.h -- drop-in C++ layer for callers of the reference's
+ * NHC_spgemm entry point (HSMU-SpGEMM), on top of the C ABI in hsmu_gb.h.
+ *
+ * A caller written against the reference (its driver, src/test.cu:10-94)
+ * includes this header instead of "NHC_spgemm.cuh", links libhsmu_gb.so and
+ * compiles unchanged:
+ *   - the operand/workspace structs keep the reference's names and fields
+ *     (NHC_CSR, NHC_mask_matrix, NHC_bin, compressed_bin, NHC_tile:
+ *     inc/NHC_spgemm.h:66-139), with index_t = int and value_t = double;
+ *   - HtD_value_col_ptr, realse_NHCcsr, realse_NHC_tile, realse_compressed_bin,
+ *     free_mask_matrix, free_C_matrix and free_bin have the reference's
+ *     signatures and release exactly what this layer allocates
+ *     (src/loading.cuh:86-174);
+ *   - NHC_spgemm(compressed_bin*, NHC_bin*, NHC_CSR *A, NHC_CSR *B, NHC_CSR *C,
+ *     NHC_mask_matrix*) (src/NHC_spgemm.cuh:7) multiplies the device copies of
+ *     A and B (d_ptr/d_col/d_val) and leaves C in C->d_ptr/d_col/d_val with
+ *     C->nnz set and the row pointers also copied to the host array
+ *     C->rowPtr, as the reference does.  Columns are sorted; values are
+ *     accumulated in FP64 in A-row order (deterministic).
+ * Errors print a message and throw std::exception, like the reference's
+ * CHECK_ERROR (inc/cuda_comm.h:16-29).  Set HSMU_VERBOSE=1 to print the
+ * per-stage times of each call.
+ */
+#ifndef HSMU_NHC_COMPAT_H
+#define HSMU_NHC_COMPAT_H
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <exception>
+
+#include "hsmu_gb.h"
+
+#ifndef value_t
+#define value_t double
+#endif
+#ifndef index_t
+#define index_t int
+#endif
+#ifndef DateTypeStoreMask
+#define DateTypeStoreMask unsigned long long
+#endif
+#ifndef DateTypeStoreCompressMask
+#define DateTypeStoreCompressMask unsigned long long
+#endif
+
+typedef struct {
+    index_t *rowPtr;
+    index_t *col;
+    value_t *val;
+    index_t *d_ptr;
+    index_t *d_col;
+    value_t *d_val;
+    index_t *d_tem_ptr;
+    int M;
+    int N;
+    index_t nnz;
+    int nnz_max;
+    int isSymmetric;
+    char *matrix_name;
+    index_t *d_tile_ptr;
+    index_t *d_tile_col;
+    index_t *d_tem_tile_ptr;
+    index_t *tile_ptr;
+    DateTypeStoreCompressMask *d_mask_num;
+} NHC_CSR;
+
+typedef struct {
+    DateTypeStoreMask *mask_matrix;
+    DateTypeStoreMask *after_or_mask_matrix;
+    int shift_of_pitch;
+    int pitch;
+    int *d_nums_over_limit_hashtable;
+    int nums_over_limit_hashtable;
+    int *d_array_store_Crow_id_over_limit;
+    int num_unit;
+    int *d_Brow_id;
+    int size_arr[5] = {12288, 24576, 49152, 98304, 196608};
+} NHC_mask_matrix;
+
+typedef struct {
+    int *bin;
+    int *d_bin;
+    int max_rows_partion;
+    int num_of_partion;
+    int *d_max_nnz_in_onerow;
+} NHC_bin;
+
+typedef struct {
+    int num_of_partion;
+    int *bin_size;
+    int *bin_offset;
+    int *max_row_nnz;
+    int *total_nnz;
+    int *bins;
+    int *d_bins;
+    int *d_bin_size;
+    int *d_bin_offset;
+    int *d_total_nnz;
+    int *d_max_row_nnz;
+    cudaStream_t *streams;
+    int *d_global_mem_pool;
+    size_t global_mem_pool_size;
+    bool global_mem_pool_malloced;
+    void *d_temp_storage;
+    size_t temp_storage_bytes = 0;
+} compressed_bin;
+
+typedef struct {
+    int *d_tile_ptr;
+    int *d_tile_col;
+    int *d_tem_tile_ptr;
+    int *tile_ptr;
+    DateTypeStoreCompressMask *d_mask_num;
+} NHC_tile;
+
+namespace hsmu_compat {
+
+inline void fail(const char *what, int status) {
+    std::printf("%s failed: %s\n", what, hsmu_strerror(status));
+    throw std::exception();
+}
+
+inline void check_cuda(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        std::printf("%s in %s\n", cudaGetErrorString(e), what);
+        throw std::exception();
+    }
+}
+
+// one library handle per thread, created on first use
+inline hsmu_handle handle() {
+    static thread_local hsmu_handle h = nullptr;
+    if (!h) {
+        const int rc = hsmu_handle_create(&h);
+        if (rc != HSMU_OK) fail("hsmu_handle_create", rc);
+    }
+    return h;
+}
+
+inline hsmu_csr view(const NHC_CSR *X) {
+    hsmu_csr v;
+    std::memset(&v, 0, sizeof(v));
+    v.M = X->M;
+    v.N = X->N;
+    v.nnz = X->nnz;
+    v.row_ptr = X->d_ptr;
+    v.col = X->d_col;
+    v.val = X->d_val;
+    return v;
+}
+
+}  // namespace hsmu_compat
+
+// device copies of the host arrays (src/loading.cuh:86-94)
+inline void HtD_value_col_ptr(NHC_CSR *A) {
+    using hsmu_compat::check_cuda;
+    check_cuda(cudaMalloc((void **)&A->d_ptr, sizeof(index_t) * (A->M + 1)), "cudaMalloc d_ptr");
+    check_cuda(cudaMalloc((void **)&A->d_col, sizeof(index_t) * (A->nnz > 0 ? A->nnz : 1)), "cudaMalloc d_col");
+    check_cuda(cudaMalloc((void **)&A->d_val, sizeof(value_t) * (A->nnz > 0 ? A->nnz : 1)), "cudaMalloc d_val");
+    check_cuda(cudaMemcpy(A->d_ptr, A->rowPtr, sizeof(index_t) * (A->M + 1), cudaMemcpyHostToDevice), "H2D row_ptr");
+    check_cuda(cudaMemcpy(A->d_col, A->col, sizeof(index_t) * A->nnz, cudaMemcpyHostToDevice), "H2D col");
+    check_cuda(cudaMemcpy(A->d_val, A->val, sizeof(value_t) * A->nnz, cudaMemcpyHostToDevice), "H2D val");
+}
+
+// C = A * B (src/NHC_spgemm.cuh:7).  B's and C's tile fields are not used by
+// this engine and stay NULL; the workspace structs are reset so that the
+// release functions below are safe to call.
+inline void NHC_spgemm(compressed_bin *cb, NHC_bin *c_bin, NHC_CSR *A, NHC_CSR *B, NHC_CSR *C,
+                       NHC_mask_matrix *mask) {
+    if (cb) {
+        std::memset((void *)cb, 0, sizeof(*cb));
+    }
+    if (c_bin) std::memset(c_bin, 0, sizeof(*c_bin));
+    if (mask) {
+        mask->mask_matrix = nullptr;
+        mask->after_or_mask_matrix = nullptr;
+        mask->d_nums_over_limit_hashtable = nullptr;
+    }
+    const hsmu_csr a = hsmu_compat::view(A), b = hsmu_compat::view(B);
+    hsmu_csr c;
+    hsmu_stats st;
+    const bool verbose = std::getenv("HSMU_VERBOSE") != nullptr;
+    const int rc = hsmu_spgemm(hsmu_compat::handle(), &a, &b, &c, nullptr, nullptr, verbose ? &st : nullptr);
+    if (rc != HSMU_OK) hsmu_compat::fail("NHC_spgemm", rc);
+    C->M = c.M;
+    C->N = c.N;
+    C->nnz = c.nnz;
+    C->d_ptr = c.row_ptr;
+    C->d_col = c.col;
+    C->d_val = c.val;
+    C->d_tile_ptr = C->d_tile_col = C->d_tem_tile_ptr = C->tile_ptr = nullptr;
+    C->d_mask_num = nullptr;
+    C->d_tem_ptr = nullptr;
+    C->rowPtr = new index_t[C->M + 1];
+    hsmu_compat::check_cuda(
+        cudaMemcpy(C->rowPtr, C->d_ptr, sizeof(index_t) * (C->M + 1), cudaMemcpyDeviceToHost), "D2H C row_ptr");
+    B->d_tile_ptr = B->d_tile_col = B->d_tem_tile_ptr = B->tile_ptr = nullptr;
+    B->d_mask_num = nullptr;
+    if (verbose)
+        std::printf("NHC_spgemm (GB300 engine): %.3f ms (conversion %.3f, symbolic %.3f, structure %.3f, "
+                    "values %.3f), products %llu, nnz(C) %lld\n",
+                    st.ms_total, st.ms_convert, st.ms_symbolic, st.ms_structure, st.ms_numeric,
+                    (unsigned long long)st.products, (long long)st.nnz_c);
+}
+
+// releases (src/loading.cuh:95-174)
+inline void realse_NHC_tile(NHC_CSR *tile) {
+    cudaFree(tile->d_tile_ptr);
+    cudaFree(tile->d_mask_num);
+    cudaFree(tile->d_tile_col);
+    delete[] tile->tile_ptr;
+    tile->d_tile_ptr = tile->d_tile_col = tile->tile_ptr = nullptr;
+    tile->d_mask_num = nullptr;
+}
+
+inline void realse_compressed_bin(compressed_bin *cb) {
+    cudaFree(cb->d_bin_size);
+    cudaFree(cb->d_bins);
+    cudaFree(cb->d_bin_offset);
+    delete[] cb->bin_offset;
+    delete[] cb->bin_size;
+    delete[] cb->bins;
+    delete[] cb->streams;
+    cudaFree(cb->d_temp_storage);
+    std::memset((void *)cb, 0, sizeof(*cb));
+}
+
+inline void realse_NHCcsr(NHC_CSR *A) {
+    cudaFree(A->d_ptr);
+    cudaFree(A->d_col);
+    cudaFree(A->d_val);
+    delete[] A->rowPtr;
+    delete[] A->col;
+    delete[] A->val;
+    A->d_ptr = A->d_col = nullptr;
+    A->d_val = nullptr;
+    A->rowPtr = A->col = nullptr;
+    A->val = nullptr;
+}
+
+inline void free_mask_matrix(NHC_mask_matrix *m) {
+    cudaFree(m->mask_matrix);
+    cudaFree(m->after_or_mask_matrix);
+    cudaFree(m->d_nums_over_limit_hashtable);
+}
+
+inline void free_C_matrix(NHC_CSR *C) {
+    hsmu_csr c;
+    std::memset(&c, 0, sizeof(c));
+    c.owned = 1;
+    c.row_ptr = C->d_ptr;
+    c.col = C->d_col;
+    c.val = C->d_val;
+    hsmu_csr_free(&c);
+    delete[] C->rowPtr;
+    C->d_ptr = C->d_col = nullptr;
+    C->d_val = nullptr;
+    C->rowPtr = nullptr;
+}
+
+inline void free_bin(NHC_bin *b) {
+    delete[] b->bin;
+    cudaFree(b->d_bin);
+    b->bin = nullptr;
+    b->d_bin = nullptr;
+}
+
+#endif /* HSMU_NHC_COMPAT_H */
