@@ -43,6 +43,19 @@ FALLBACK_HBM_GBS = 6800.0
 FP64_LANE_OPS_PER_S = 5.06e11
 # DRAM bytes (read + write) per launch of the dominant kernel, from ncu captures
 # summarised under profiles/ (null until captured for a workload).
+class HostCSR:
+    """host CSR operand of hsmu_spgemm_host (page-locked torch tensors)"""
+
+    def __init__(self, M, N, row_ptr, col, val):
+        self.M, self.N, self.row_ptr, self.col, self.val = M, N, row_ptr, col, val
+
+    def nbytes(self):
+        return sum(x.numel() * x.element_size() for x in (self.row_ptr, self.col, self.val))
+
+
+# hsmu_opts.arith of the --arith choices
+ARITH = {"rn": 0, "fma": 1, "imul": 2}
+
 TRAFFIC = {
     # profiles/k_struct_ds_stencil27_32_dof3.md: 447.3 MB on the 32^3 case, scaled by the
     # algorithmic bytes (x1.993) to the 40^3 workload
@@ -258,7 +271,7 @@ def run_engine(args):
     # warm-up (also gives nnz(C) for the e2e host buffers)
     nnz_c = 0
     for _ in range(args.warmup):
-        C = eng.spgemm(dA, dB, stats=True)
+        C = eng.spgemm(dA, dB, stats=True, arith=ARITH[args.arith])
         nnz_c = C.nnz
         C.free()
     torch.cuda.synchronize()
@@ -274,7 +287,7 @@ def run_engine(args):
     stage = {k: 0.0 for k in ("ms_convert", "ms_symbolic", "ms_alloc", "ms_structure", "ms_numeric")}
     launches = 0
     for _ in range(args.steps):
-        C = eng.spgemm(dA, dB, stats=True)
+        C = eng.spgemm(dA, dB, stats=True, arith=ARITH[args.arith])
         st = eng.last_stats
         for k in stage:
             stage[k] += st[k]
@@ -288,36 +301,19 @@ def run_engine(args):
     ms = dist_max(ms, world)
     value = world * 2.0 * products / (ms * 1e-3) / 1e9
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the public host-buffer call (hsmu_spgemm_host): page-locked
+    # host operands in, host CSR out; the copies run inside the call, behind the compute
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-    hA = (pin(A.row_ptr), pin(A.col), pin(A.val))
-    hB = hA if same else (pin(B.row_ptr), pin(B.col), pin(B.val))
-    gA = tuple(torch.empty_like(x, device="cuda") for x in hA)
-    gB = gA if same else tuple(torch.empty_like(x, device="cuda") for x in hB)
+    hA = HostCSR(A.M, A.N, pin(A.row_ptr), pin(A.col), pin(A.val))
+    hB = hA if same else HostCSR(B.M, B.N, pin(B.row_ptr), pin(B.col), pin(B.val))
     oC = (torch.empty(A.M + 1, dtype=torch.int32).pin_memory(),
           torch.empty(nnz_c, dtype=torch.int32).pin_memory(),
           torch.empty(nnz_c, dtype=torch.float64).pin_memory())
-    h2d = sum(x.numel() * x.element_size() for x in hA) + (0 if same else sum(
-        x.numel() * x.element_size() for x in hB))
+    h2d = hA.nbytes() + (0 if same else hB.nbytes())
     d2h = sum(x.numel() * x.element_size() for x in oC)
-    L = hsmu_gb.load_library()
 
     def e2e_step():
-        for g, h in zip(gA, hA):
-            g.copy_(h, non_blocking=True)
-        if not same:
-            for g, h in zip(gB, hB):
-                g.copy_(h, non_blocking=True)
-        dA2 = hsmu_gb.DeviceCSR.from_tensors(A.M, A.N, *gA)
-        dB2 = dA2 if same else hsmu_gb.DeviceCSR.from_tensors(B.M, B.N, *gB)
-        C = eng.spgemm(dA2, dB2)
-        import ctypes
-
-        rc = L.hsmu_csr_download(ctypes.byref(C.desc), oC[0].data_ptr(), oC[1].data_ptr(),
-                                 oC[2].data_ptr(), ctypes.c_void_p(stream.cuda_stream))
-        if rc:
-            raise RuntimeError("download failed %d" % rc)
-        C.free()
+        eng.spgemm_host(hA, hB, out=oC, arith=ARITH[args.arith], stream=stream)
 
     e2e_step()
     torch.cuda.synchronize()
@@ -347,7 +343,9 @@ def run_engine(args):
     else:
         kname, kms = "k_numeric (values, per window)", nu_ms
     achieved = alg_bytes / (kms * 1e-3) / 1e9
-    fp64_ach = 2.0 * products / (kms * 1e-3)  # FP64 lane-ops/s (one DMUL + one DADD per product)
+    # FP64 lane-ops/s: one DMUL + one DADD per product (rn), one DFMA (fma), one DADD (imul)
+    fp64_per_product = {"rn": 2.0, "fma": 1.0, "imul": 1.0}[args.arith]
+    fp64_ach = fp64_per_product * products / (kms * 1e-3)
     traffic = TRAFFIC.get(args.workload)
 
     if rank != 0:
@@ -362,7 +360,7 @@ def run_engine(args):
                    "nnz_A": A.nnz, "nnz_B": B.nnz, "nnz_C": nnz_c, "products": products,
                    "l2": "inputs and output larger than L2 (A %.0f MB, C %.0f MB > 129 MB)" % (
                        csr_bytes(A.M, A.nnz) / 1e6, csr_bytes(A.M, nnz_c) / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "arith": args.arith},
         "hbm_gbs_step": round(alg_bytes / (ms * 1e-3) / 1e9, 2),
         "stages_ms": {k: round(v / args.steps, 4) for k, v in stage.items()},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 2),
@@ -371,7 +369,7 @@ def run_engine(args):
                      "alg_bytes": alg_bytes, "ms": round(kms, 4)},
         "fp64_pipe": {"achieved_lane_ops_per_s": fp64_ach, "peak_lane_ops_per_s": FP64_LANE_OPS_PER_S,
                       "frac": round(fp64_ach / FP64_LANE_OPS_PER_S, 4),
-                      "note": "the value pass is bound by the FP64 pipe: one DMUL + one DADD per product"},
+                      "note": "FP64 pipe lane-ops of the value pass (rn: DMUL + DADD per product; fma: one DFMA; imul: one DADD)"},
         "cpu_baseline": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in cpu.items()
                          if k != "seconds"},
         "e2e": {"value": round(e2e_value, 3), "unit": "GFLOPS", "ms_per_step": round(e2e_ms, 4),
@@ -525,6 +523,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--workload", default="stencil27_40_dof3_AA", choices=sorted(WORKLOADS))
+    ap.add_argument("--arith", default="rn", choices=sorted(ARITH),
+                    help="accumulation: rn = product rounded then added (the reference's arithmetic), "
+                         "fma = one fused multiply-add per product, imul = rn with integer-pipe multiply")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -82,7 +82,7 @@ struct BParams {
     long long *bsum;       // [gridDim.x + 1]
     GridBar *bar;
     int *err;
-    int int_mul;
+    int arith;             // hsmu_opts.arith of the batch
 };
 
 __device__ bool grid_sync(GridBar *gb, int *err) {
@@ -159,7 +159,7 @@ struct BWarpSmem {
     };
 };
 
-template <bool INT_MUL, bool FILL, bool NC>
+template <int AR, bool FILL, bool NC>
 __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
     const BRound &R = P.rnd[r];
     const int lane = lane_id(), w = threadIdx.x >> 5;
@@ -188,9 +188,9 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
                 const long long o = R.excl[i];
                 const int nnz = R.cnnz[i];
                 if (o + nnz <= R.cap) {
-                    const int got = tiny_row_fill<NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val, S.t.cols + lane,
-                                                      S.t.acc + lane, WARP, nnz, R.col_pool + o, R.val_pool + o,
-                                                      [](double x, double y) { return prod_mul<INT_MUL>(x, y); });
+                    const int got = tiny_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val,
+                                                          S.t.cols + lane, S.t.acc + lane, WARP, nnz, R.col_pool + o,
+                                                          R.val_pool + o);
                     if (got != nnz) atomicOr(P.err, BERR_INTERNAL);
                 }
             }
@@ -227,7 +227,7 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
                 const long long o = R.excl[ib];
                 const int nnz = R.cnnz[ib];
                 if (nnz <= B_FUSE_CAP && o + nnz <= R.cap) {
-                    if (!warp_row_fill<INT_MUL, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val, t0, span, S.w.msk,
+                    if (!warp_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val, t0, span, S.w.msk,
                                                 S.w.base, S.w.acc, nnz, R.col_pool + o, R.val_pool + o) &&
                         lane == 0)
                         atomicOr(P.err, BERR_INTERNAL);
@@ -295,21 +295,21 @@ __device__ void phase_rowptr(const BParams &P, int r) {
         if (R.row0[p + 1] == R.row0[p]) R.rp_pool[R.rpo[p]] = 0;
 }
 
-template <bool INT_MUL>
+template <int AR>
 __global__ void __launch_bounds__(BW * 32) k_batch(BParams P) {
     extern __shared__ unsigned long long s_dyn[];
     BWarpSmem &S = reinterpret_cast<BWarpSmem *>(s_dyn)[threadIdx.x >> 5];
     for (int r = 0; r < P.nrounds; r++) {
         if (r > 0 && !grid_sync(P.bar, P.err)) return;
-        if (r == 0) phase_rows<INT_MUL, false, true>(P, r, S);
-        else phase_rows<INT_MUL, false, false>(P, r, S);
+        if (r == 0) phase_rows<AR, false, true>(P, r, S);
+        else phase_rows<AR, false, false>(P, r, S);
         if (!grid_sync(P.bar, P.err)) return;
         if (!phase_scan(P, r)) return;
         if (!grid_sync(P.bar, P.err)) return;
         if (*(volatile int *)P.err & BERR_CAPACITY) return;
         phase_rowptr(P, r);
-        if (r == 0) phase_rows<INT_MUL, true, true>(P, r, S);
-        else phase_rows<INT_MUL, true, false>(P, r, S);
+        if (r == 0) phase_rows<AR, true, true>(P, r, S);
+        else phase_rows<AR, true, false>(P, r, S);
     }
 }
 
@@ -358,7 +358,7 @@ using namespace hsmu;
 
 struct hsmu_batch_s {
     int kind, nprod;
-    int nsm, grid, threads, tiny, int_mul;
+    int nsm, grid, threads, tiny, arith;
     size_t smem;
     BParams P;
     // device allocations
@@ -394,19 +394,20 @@ int launch_batch(hsmu_batch_s *b, cudaStream_t st) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = b->int_mul ? cudaLaunchKernelEx(&cfg, k_batch<true>, b->P)
-                               : cudaLaunchKernelEx(&cfg, k_batch<false>, b->P);
+    cudaError_t e = b->arith == AR_IMUL  ? cudaLaunchKernelEx(&cfg, k_batch<AR_IMUL>, b->P)
+                    : b->arith == AR_FMA ? cudaLaunchKernelEx(&cfg, k_batch<AR_FMA>, b->P)
+                                         : cudaLaunchKernelEx(&cfg, k_batch<AR_RN>, b->P);
     return e == cudaSuccess ? HSMU_OK : HSMU_ERR_CUDA;
 }
 
 int configure_batch(hsmu_batch_s *b, int dev) {
     b->threads = BW * 32;
     b->smem = BW * sizeof(BWarpSmem);
-    int e = (int)cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
-    if (!e) e = (int)cudaFuncSetAttribute(k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
-    if (e) return HSMU_ERR_CUDA;
+    for (auto k : {k_batch<AR_RN>, k_batch<AR_FMA>, k_batch<AR_IMUL>})
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem) != cudaSuccess)
+            return HSMU_ERR_CUDA;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<false>, b->threads, b->smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<AR_RN>, b->threads, b->smem) != cudaSuccess ||
         per_sm < 1)
         return HSMU_ERR_CUDA;
     int coop = 0;
@@ -425,6 +426,7 @@ int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const h
     if (!h || !out || n <= 0 || !A || !B) return HSMU_ERR_INVALID;
     if (kind != HSMU_BATCH_PRODUCT && kind != HSMU_BATCH_GALERKIN) return HSMU_ERR_INVALID;
     if (kind == HSMU_BATCH_GALERKIN && !Pt) return HSMU_ERR_INVALID;
+    if (opts && (opts->arith < HSMU_ARITH_RN || opts->arith > HSMU_ARITH_IMUL)) return HSMU_ERR_INVALID;
     *out = nullptr;
     for (int p = 0; p < n; p++) {
         if (A[p].N != B[p].M || !A[p].row_ptr || !B[p].row_ptr) return HSMU_ERR_INVALID;
@@ -435,7 +437,7 @@ int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const h
     if (!b) return HSMU_ERR_ALLOC;
     b->kind = kind;
     b->nprod = n;
-    b->int_mul = opts && opts->arith == 2;
+    b->arith = opts ? opts->arith : AR_RN;
     b->tiny = TINY_MAX;
     int dev = 0;
     cudaGetDevice(&dev);
@@ -527,7 +529,7 @@ int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const h
         cudaFree(rowbound);
         b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), (void *)rowbound));
     }
-    b->P.int_mul = b->int_mul;
+    b->P.arith = b->arith;
     *out = b;
     return HSMU_OK;
 fail:
@@ -601,7 +603,7 @@ int hsmu_batch_set_params(hsmu_batch b, int tiny, int grid) {
     b->tiny = tiny;
     if (grid > 0) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<false>, b->threads, b->smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<AR_RN>, b->threads, b->smem);
         if (grid > b->nsm * per_sm) return HSMU_ERR_INVALID;  // cooperative launch needs all blocks resident
         b->grid = grid;
     }
@@ -620,7 +622,7 @@ int hsmu_batch_autotune(hsmu_batch b, void *stream, int *best_tiny, int *best_gr
     if (!b) return HSMU_ERR_INVALID;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<false>, b->threads, b->smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<AR_RN>, b->threads, b->smem);
     const int tinies[] = {8, 16, 32};
     std::vector<int> grids = {b->nsm * per_sm};
     if (per_sm > 1) grids.push_back(b->nsm);

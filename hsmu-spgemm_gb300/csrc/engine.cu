@@ -15,10 +15,12 @@
 // memory cached across calls.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "hsmu_gb.h"
 #include "hsmu_common.cuh"
@@ -37,6 +39,9 @@ struct hsmu_handle_s {
     int nsm;
     Ctl *h_ctl;  // pinned host mirror of the control block
     cudaEvent_t ev[8];
+    // host-buffer entry: copy streams and their ordering events
+    cudaStream_t cs_in, cs_out;
+    cudaEvent_t ev_in, ev_panel, ev_out;
 };
 
 namespace {
@@ -49,7 +54,16 @@ const char *kErr[] = {"ok",
                       "input CSR not canonical (columns must be strictly increasing and in range)",
                       "internal consistency check failed on the device",
                       "bounded device wait timed out",
-                      "no usable sm_103 device"};
+                      "no usable sm_103 device",
+                      "a batch holds rows that need the plain engine's large-row path",
+                      "output buffers too small: C->nnz holds the required number of entries"};
+
+// hsmu_spgemm_host: output bytes (columns + values) per row panel, the most
+// panels, and the ratio of consecutive panel sizes (decreasing sizes: the copy
+// of the last panel, which nothing hides, is the smallest)
+constexpr long long HOST_PANEL_BYTES = 32ll << 20;
+constexpr long long HOST_MAX_PANELS = 8;
+constexpr double HOST_PANEL_RATIO = 0.7;
 
 int from_cuda(cudaError_t e) {
     if (e == cudaSuccess) return HSMU_OK;
@@ -133,6 +147,183 @@ done:
     return rc;
 }
 
+#define CKR(x)                              \
+    do {                                    \
+        const cudaError_t _e = (x);         \
+        if (_e != cudaSuccess) return from_cuda(_e); \
+    } while (0)
+
+bool arith_ok(const hsmu_opts &o) { return o.arith >= HSMU_ARITH_RN && o.arith <= HSMU_ARITH_IMUL; }
+
+// One plain product on the device, in stages: begin (control block,
+// validation), symbolic (tiles, bounds, exact count, scan -> row pointers and
+// nnz(C), one host read), alloc_output, then structure(lo, hi) + values()
+// for one or more row panels, and finish (completion read, device checks).
+// hsmu_spgemm runs one panel of all rows; hsmu_spgemm_host runs several so
+// that copies of finished panels overlap the next panel's kernels.
+struct PlainRun {
+    hsmu_handle_s *h;
+    cudaStream_t st;
+    hsmu_opts o;
+    int M = 0;
+    DevCSR Ad{}, Bd{};
+    hsmu_btiles bt{};
+    bool own_tiles = false;
+    DevTiles Btd{};
+    RowInfo ri{};
+    int *scan_tmp = nullptr;
+    Window *win = nullptr;
+    long long win_cap = 0;
+    int *crp = nullptr, *ccol = nullptr;
+    double *cval = nullptr;
+    Ctl *ctl = nullptr;
+    Ctl hc{};
+    int launches = 0;
+
+    PlainRun(hsmu_handle_s *h_, cudaStream_t st_, const hsmu_opts &o_) : h(h_), st(st_), o(o_) {}
+    ~PlainRun() { release(); }
+
+    int begin(const hsmu_csr *A, const hsmu_csr *B) {
+        M = A->M;
+        Ad = dev(A);
+        Bd = dev(B);
+        CKR(palloc(&ctl, 1, st));
+        CKR(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+        if (o.validate) {
+            // check both operands before any kernel indexes through them
+            launch_validate(Ad, ctl, grid_rows(h), st);
+            launch_validate(Bd, ctl, grid_rows(h), st);
+            launches += 2;
+            CKR(cudaGetLastError());
+            CKR(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+            CKR(cudaStreamSynchronize(st));
+            if (h->h_ctl->err) return err_from_dev(h->h_ctl->err);
+        }
+        return HSMU_OK;
+    }
+
+    // host_rp != NULL: the row pointers of C are copied there in the same host read
+    int symbolic(const hsmu_csr *B, const hsmu_btiles *Bt_in, bool count_tiles, int32_t *host_rp,
+                 cudaEvent_t ev_tiles) {
+        if (Bt_in) {
+            bt = *Bt_in;
+        } else {
+            const int rc = build_tiles(h, B, &bt, ctl, 0, st, count_tiles);
+            if (rc) return rc;
+            own_tiles = true;
+            launches += 5;
+        }
+        Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
+        if (ev_tiles) cudaEventRecord(ev_tiles, st);
+        CKR(palloc(&ri.prod, (size_t)M, st));
+        CKR(palloc(&ri.tmin, (size_t)M, st));
+        CKR(palloc(&ri.tmax, (size_t)M, st));
+        CKR(palloc(&ri.bins, (size_t)M * NBIN, st));
+        CKR(palloc(&ri.cls, (size_t)M, st));
+        CKR(palloc(&ri.bin_cnt, bin_scratch_ints(M), st));
+        CKR(palloc(&ri.cnnz, (size_t)M + 1, st));
+        CKR(palloc(&scan_tmp, scan_tmp_ints(M), st));
+        CKR(palloc(&crp, (size_t)M + 1, st));
+        launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
+        launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
+        launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
+        launches += 12;  // bounds + binning 6, count 3, scan 3
+        CKR(cudaGetLastError());
+        CKR(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        if (host_rp) CKR(cudaMemcpyAsync(host_rp, crp, sizeof(int32_t) * ((size_t)M + 1), cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+        hc = *h->h_ctl;
+        if (hc.err) return err_from_dev(hc.err);
+        if (hc.nnz > INT_MAX) return HSMU_ERR_OVERFLOW;
+        win_cap = (long long)hc.win_bound;
+        if (win_cap > INT_MAX) return HSMU_ERR_OVERFLOW;
+        return HSMU_OK;
+    }
+
+    int alloc_output() {
+        CKR(palloc(&ccol, (size_t)hc.nnz, st));
+        CKR(palloc(&cval, (size_t)hc.nnz, st));
+        CKR(palloc(&win, (size_t)win_cap, st));
+        return HSMU_OK;
+    }
+
+    // sorted columns of rows lo..hi-1, values of warp-sized rows, numeric windows of the others
+    void structure(int lo, int hi) {
+        if (hc.nnz == 0) return;
+        launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_PLAIN, crp, nullptr, ccol, cval, nullptr, nullptr, lo, hi}, win,
+                         win_cap, ctl, o.arith, h->nsm, st);
+        launches += 3;
+    }
+
+    // values of the windows made by the preceding structure() call
+    void values() {
+        if (hc.nnz == 0) return;
+        launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, ctl, o.arith, h->nsm, st);
+        launches += 1;
+    }
+
+    // start a new panel: its windows reuse the window buffer from slot 0
+    int next_panel() {
+        CKR(cudaMemsetAsync(&ctl->win_count, 0, sizeof(int), st));
+        return HSMU_OK;
+    }
+
+    // completion + device-side checks
+    int finish() {
+        CKR(cudaGetLastError());
+        CKR(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+        hc = *h->h_ctl;
+        return hc.err ? err_from_dev(hc.err) : HSMU_OK;
+    }
+
+    void release() {
+        pfree(ctl, st);
+        if (own_tiles) {
+            pfree(bt.tile_ptr, st);
+            pfree(bt.tile_col, st);
+            pfree(bt.mask, st);
+            pfree(bt.tile_off, st);
+            own_tiles = false;
+        }
+        pfree(ri.prod, st);
+        pfree(ri.tmin, st);
+        pfree(ri.tmax, st);
+        pfree(ri.bins, st);
+    pfree(ri.cls, st);
+    pfree(ri.bin_cnt, st);
+        pfree(ri.cls, st);
+        pfree(ri.bin_cnt, st);
+        pfree(ri.cnnz, st);
+        pfree(scan_tmp, st);
+        pfree(win, st);
+        pfree(crp, st);
+        pfree(ccol, st);
+        pfree(cval, st);
+    }
+};
+
+void fill_stats(hsmu_handle_s *h, const PlainRun &r, const hsmu_btiles *Bt_in, hsmu_stats *stats) {
+    float t;
+    stats->products = r.hc.products;
+    stats->nnz_c = r.hc.nnz;
+    stats->ntiles_b = Bt_in ? Bt_in->ntiles : r.hc.ntiles;
+    stats->windows = r.hc.win_count;
+    cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
+    stats->ms_convert = t;
+    cudaEventElapsedTime(&t, h->ev[1], h->ev[2]);
+    stats->ms_symbolic = t;
+    cudaEventElapsedTime(&t, h->ev[2], h->ev[3]);
+    stats->ms_alloc = t;
+    cudaEventElapsedTime(&t, h->ev[3], h->ev[4]);
+    stats->ms_structure = t;
+    cudaEventElapsedTime(&t, h->ev[4], h->ev[5]);
+    stats->ms_numeric = t;
+    cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
+    stats->ms_total = t;
+    stats->launches = r.launches;
+}
+
 int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hsmu_btiles *Bt_in, hsmu_csr *C,
                 const hsmu_opts *opts, cudaStream_t st, hsmu_stats *stats) {
     if (!h || !csr_ok(A) || !csr_ok(B) || !C) return HSMU_ERR_INVALID;
@@ -140,158 +331,180 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
     if (Bt_in && (Bt_in->M != B->M || Bt_in->N != B->N || !Bt_in->tile_ptr)) return HSMU_ERR_INVALID;
     hsmu_opts o{};
     if (opts) o = *opts;
-    const int M = A->M;
-    int rc = HSMU_OK;
-    Ctl *ctl = nullptr;
-    hsmu_btiles bt{};
-    bool own_tiles = false;
-    RowInfo ri{};
-    int *scan_tmp = nullptr;
-    Window *win = nullptr;
-    long long win_cap = 0;
-    int *crp = nullptr, *ccol = nullptr;
-    double *cval = nullptr;
-    Ctl hc{};
-    DevCSR Ad = dev(A), Bd = dev(B);
-    DevTiles Btd{};
+    if (!arith_ok(o)) return HSMU_ERR_INVALID;
     std::memset(C, 0, sizeof(*C));
-
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         cudaEventRecord(h->ev[0], st);
     }
-    CK(palloc(&ctl, 1, st));
-    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
-    if (o.validate) {
-        // check both operands before any kernel indexes through them
-        launch_validate(Ad, ctl, grid_rows(h), st);
-        launch_validate(Bd, ctl, grid_rows(h), st);
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (h->h_ctl->err) {
-            rc = err_from_dev(h->h_ctl->err);
-            goto done;
+    PlainRun r(h, st, o);
+    int rc = r.begin(A, B);
+    if (!rc) rc = r.symbolic(B, Bt_in, stats != nullptr, nullptr, stats ? h->ev[1] : nullptr);
+    if (!rc && stats) cudaEventRecord(h->ev[2], st);
+    if (!rc) rc = r.alloc_output();
+    if (!rc) {
+        if (stats) cudaEventRecord(h->ev[3], st);
+        r.structure(0, A->M);
+        if (stats) cudaEventRecord(h->ev[4], st);
+        r.values();
+        if (stats) cudaEventRecord(h->ev[5], st);
+        rc = r.finish();
+    }
+    if (rc != HSMU_OK) {
+        r.release();
+        cudaStreamSynchronize(st);
+        return rc;
+    }
+    C->M = A->M;
+    C->N = B->N;
+    C->nnz = (int32_t)r.hc.nnz;
+    C->owned = 1;
+    C->row_ptr = r.crp;
+    C->col = r.ccol;
+    C->val = r.cval;
+    r.crp = nullptr;
+    r.ccol = nullptr;
+    r.cval = nullptr;
+    if (stats) fill_stats(h, r, Bt_in, stats);
+    return HSMU_OK;
+}
+
+// Host-buffer product with the output copy pipelined behind the compute.
+//   copy stream in:  values of B (and A), while tiles/bounds/count run on `st`
+//   st:              symbolic pass, one host read (nnz and the row pointers,
+//                    straight into C->row_ptr), then row panels of about
+//                    equal nnz: structure + values of panel q
+//   copy stream out: columns and values of panel q while panel q+1 computes
+// (Stores from the kernels straight into page-locked host memory measured
+// 2.8x slower than this on GB300: the fused kernel's row-sized writes go out
+// over the CPU link at a fraction of its copy bandwidth.)
+// The result is the same as hsmu_spgemm followed by a download.
+int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_opts *opts,
+                     cudaStream_t st, hsmu_stats *stats) {
+    if (!h || !csr_ok(A) || !csr_ok(B) || !C || !C->row_ptr) return HSMU_ERR_INVALID;
+    if (A->N != B->M || C->nnz < 0 || (C->nnz > 0 && (!C->col || !C->val))) return HSMU_ERR_INVALID;
+    hsmu_opts o{};
+    if (opts) o = *opts;
+    if (!arith_ok(o) || o.panels < 0) return HSMU_ERR_INVALID;
+    const long long capacity = C->nnz;
+    const bool same = A->row_ptr == B->row_ptr && A->col == B->col && A->val == B->val && A->M == B->M &&
+                      A->N == B->N && A->nnz == B->nnz;
+    const int M = A->M;
+    int rc = HSMU_OK;
+    hsmu_csr dA{}, dB{};
+    PlainRun r(h, st, o);
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        cudaEventRecord(h->ev[0], st);
+    }
+    auto upload = [&](const hsmu_csr *X, hsmu_csr *D) -> int {
+        *D = *X;
+        D->owned = 0;
+        D->row_ptr = nullptr;
+        D->col = nullptr;
+        D->val = nullptr;
+        CKR(palloc(&D->row_ptr, (size_t)X->M + 1, st));
+        CKR(palloc(&D->col, (size_t)X->nnz, st));
+        CKR(palloc(&D->val, (size_t)X->nnz, st));
+        // index arrays on st (the symbolic pass needs them first) ...
+        CKR(cudaMemcpyAsync(D->row_ptr, X->row_ptr, sizeof(int32_t) * ((size_t)X->M + 1), cudaMemcpyHostToDevice, st));
+        if (X->nnz) CKR(cudaMemcpyAsync(D->col, X->col, sizeof(int32_t) * (size_t)X->nnz, cudaMemcpyHostToDevice, st));
+        // ... values on the input copy stream, behind the symbolic pass
+        CKR(cudaEventRecord(h->ev_in, st));
+        CKR(cudaStreamWaitEvent(h->cs_in, h->ev_in, 0));
+        if (X->nnz)
+            CKR(cudaMemcpyAsync(D->val, X->val, sizeof(double) * (size_t)X->nnz, cudaMemcpyHostToDevice, h->cs_in));
+        return HSMU_OK;
+    };
+    std::vector<int> cut;
+    rc = upload(B, &dB);
+    if (!rc) {
+        if (same) dA = dB;
+        else rc = upload(A, &dA);
+    }
+    if (!rc) CK(cudaEventRecord(h->ev_in, h->cs_in));
+    if (!rc) rc = r.begin(&dA, &dB);
+    if (!rc) rc = r.symbolic(&dB, nullptr, stats != nullptr, C->row_ptr, stats ? h->ev[1] : nullptr);
+    if (!rc && stats) cudaEventRecord(h->ev[2], st);
+    if (!rc && r.hc.nnz > capacity) {
+        // report the size; the row pointers are already in C->row_ptr
+        C->M = M;
+        C->N = B->N;
+        C->nnz = (int32_t)r.hc.nnz;
+        rc = HSMU_ERR_CAPACITY;
+    }
+    if (!rc) rc = r.alloc_output();
+    if (!rc) {
+        if (stats) cudaEventRecord(h->ev[3], st);
+        CK(cudaStreamWaitEvent(st, h->ev_in, 0));  // values of A and B are on the device
+        const long long nnz = r.hc.nnz;
+        long long np = o.panels > 0 ? o.panels : (nnz * 12 + HOST_PANEL_BYTES - 1) / HOST_PANEL_BYTES;
+        np = np < 1 ? 1 : (np > HOST_MAX_PANELS ? HOST_MAX_PANELS : np);
+        if (np > M) np = M > 0 ? M : 1;
+        // panel q = rows [cut[q], cut[q+1]): the first row whose entries start at or after the
+        // panel's share of nnz; shares shrink geometrically (HOST_PANEL_RATIO) from the first panel
+        cut.push_back(0);
+        double wsum = 0.0, w = 1.0;
+        for (long long q = 0; q < np; q++, w *= HOST_PANEL_RATIO) wsum += w;
+        double acc = 0.0;
+        w = 1.0;
+        for (long long q = 1; q < np; q++, w *= HOST_PANEL_RATIO) {
+            acc += w;
+            const long long target = (long long)((double)nnz * (acc / wsum));
+            const int row = (int)(std::lower_bound(C->row_ptr, C->row_ptr + M + 1, (int32_t)target) - C->row_ptr);
+            cut.push_back(row < cut.back() ? cut.back() : (row > M ? M : row));
         }
+        cut.push_back(M);
+        for (size_t q = 0; q + 1 < cut.size(); q++) {
+            const int lo = cut[q], hi = cut[q + 1];
+            if (lo == hi) continue;
+            if (q > 0) {
+                rc = r.next_panel();
+                if (rc) break;
+            }
+            r.structure(lo, hi);
+            r.values();
+            const long long e0 = C->row_ptr[lo], e1 = C->row_ptr[hi];
+            if (e1 == e0) continue;
+            CK(cudaEventRecord(h->ev_panel, st));
+            CK(cudaStreamWaitEvent(h->cs_out, h->ev_panel, 0));
+            CK(cudaMemcpyAsync(C->col + e0, r.ccol + e0, sizeof(int32_t) * (size_t)(e1 - e0), cudaMemcpyDeviceToHost,
+                               h->cs_out));
+            CK(cudaMemcpyAsync(C->val + e0, r.cval + e0, sizeof(double) * (size_t)(e1 - e0), cudaMemcpyDeviceToHost,
+                               h->cs_out));
+        }
+        if (stats) cudaEventRecord(h->ev[4], st);
+        if (!rc) CK(cudaEventRecord(h->ev_out, h->cs_out));
+        if (!rc) CK(cudaStreamWaitEvent(st, h->ev_out, 0));
+        if (stats) cudaEventRecord(h->ev[5], st);
+        if (!rc) rc = r.finish();
     }
-
-    // 1. B tiles
-    if (Bt_in) {
-        bt = *Bt_in;
-    } else {
-        rc = build_tiles(h, B, &bt, ctl, 0, st, stats != nullptr);
-        if (rc) goto done;
-        own_tiles = true;
+done:
+    // copies still in flight on the copy streams finish before their buffers go
+    cudaStreamSynchronize(h->cs_in);
+    cudaStreamSynchronize(h->cs_out);
+    r.release();
+    if (dA.row_ptr && dA.row_ptr != dB.row_ptr) {
+        pfree(dA.row_ptr, st);
+        pfree(dA.col, st);
+        pfree(dA.val, st);
     }
-    Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
-    if (stats) cudaEventRecord(h->ev[1], st);
-
-    // 2. bounds and bins
-    CK(palloc(&ri.prod, (size_t)M, st));
-    CK(palloc(&ri.tmin, (size_t)M, st));
-    CK(palloc(&ri.tmax, (size_t)M, st));
-    CK(palloc(&ri.bins, (size_t)M * NBIN, st));
-    CK(palloc(&ri.cnnz, (size_t)M + 1, st));
-    CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
-    CK(palloc(&crp, (size_t)M + 1, st));
-    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
-    // 3. exact count
-    launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
-    // 4. scan -> row_ptr, nnz
-    launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    hc = *h->h_ctl;
-    if (stats) cudaEventRecord(h->ev[2], st);
-    if (hc.err) {
-        rc = err_from_dev(hc.err);
-        goto done;
-    }
-    if (hc.nnz > INT_MAX) {
-        rc = HSMU_ERR_OVERFLOW;
-        goto done;
-    }
-    win_cap = (long long)hc.win_bound;
-    if (win_cap > INT_MAX) {
-        rc = HSMU_ERR_OVERFLOW;
-        goto done;
-    }
-    CK(palloc(&ccol, (size_t)hc.nnz, st));
-    CK(palloc(&cval, (size_t)hc.nnz, st));
-    CK(palloc(&win, (size_t)win_cap, st));
-    if (stats) cudaEventRecord(h->ev[3], st);
-
-    // 5a. structure + windows
-    if (hc.nnz > 0)
-        launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_PLAIN, crp, nullptr, ccol, cval, nullptr, nullptr}, win, win_cap,
-                         ctl, o.arith, h->nsm, st);
-    if (stats) cudaEventRecord(h->ev[4], st);
-    // 5b. values
-    if (hc.nnz > 0)
-        launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, ctl, o.arith, h->nsm, st);
-    CK(cudaGetLastError());
-    if (stats) cudaEventRecord(h->ev[5], st);
-
-    // completion + device-side checks
-    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    hc = *h->h_ctl;
-    if (hc.err) {
-        rc = err_from_dev(hc.err);
-        goto done;
+    pfree(dB.row_ptr, st);
+    pfree(dB.col, st);
+    pfree(dB.val, st);
+    if (rc != HSMU_OK) {
+        cudaStreamSynchronize(st);
+        return rc;
     }
     C->M = M;
     C->N = B->N;
-    C->nnz = (int32_t)hc.nnz;
-    C->owned = 1;
-    C->row_ptr = crp;
-    C->col = ccol;
-    C->val = cval;
-    crp = nullptr;
-    ccol = nullptr;
-    cval = nullptr;
+    C->nnz = (int32_t)r.hc.nnz;
+    C->owned = 0;
     if (stats) {
-        float t;
-        stats->products = hc.products;
-        stats->nnz_c = hc.nnz;
-        stats->ntiles_b = Bt_in ? Bt_in->ntiles : hc.ntiles;
-        stats->windows = hc.win_count;
-        cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
-        stats->ms_convert = t;
-        cudaEventElapsedTime(&t, h->ev[1], h->ev[2]);
-        stats->ms_symbolic = t;
-        cudaEventElapsedTime(&t, h->ev[2], h->ev[3]);
-        stats->ms_alloc = t;
-        cudaEventElapsedTime(&t, h->ev[3], h->ev[4]);
-        stats->ms_structure = t;
-        cudaEventElapsedTime(&t, h->ev[4], h->ev[5]);
-        stats->ms_numeric = t;
-        cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
-        stats->ms_total = t;
-        // validate 2, tiles 5 (count, 3 scan, fill), bounds 1, count 3, scan 3, structure 3, numeric 1
-        stats->launches = (o.validate ? 2 : 0) + (Bt_in ? 0 : 5) + 7 + (hc.nnz > 0 ? 4 : 0);
+        fill_stats(h, r, nullptr, stats);
+        stats->launches = r.launches;
     }
-done:
-    pfree(ctl, st);
-    if (own_tiles) {
-        pfree(bt.tile_ptr, st);
-        pfree(bt.tile_col, st);
-        pfree(bt.mask, st);
-        pfree(bt.tile_off, st);
-    }
-    pfree(ri.prod, st);
-    pfree(ri.tmin, st);
-    pfree(ri.tmax, st);
-    pfree(ri.bins, st);
-    pfree(ri.cnnz, st);
-    pfree(scan_tmp, st);
-    pfree(win, st);
-    pfree(crp, st);
-    pfree(ccol, st);
-    pfree(cval, st);
-    if (rc != HSMU_OK) cudaStreamSynchronize(st);
-    return rc;
+    return HSMU_OK;
 }
 
 // Learned path (see learned.cu): predicted slots instead of the exact count pass.
@@ -301,6 +514,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     if (A->N != B->M) return HSMU_ERR_INVALID;
     hsmu_opts o{};
     if (opts) o = *opts;
+    if (o.arith < HSMU_ARITH_RN || o.arith > HSMU_ARITH_IMUL) return HSMU_ERR_INVALID;
     const int M = A->M;
     int rc = HSMU_OK;
     Ctl *ctl = nullptr;
@@ -342,6 +556,8 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     CK(palloc(&ri.tmin, (size_t)M, st));
     CK(palloc(&ri.tmax, (size_t)M, st));
     CK(palloc(&ri.bins, (size_t)M * NBIN, st));
+    CK(palloc(&ri.cls, (size_t)M, st));
+    CK(palloc(&ri.bin_cnt, bin_scratch_ints(M), st));
     CK(palloc(&ri.cnnz, (size_t)M + 1, st));
     CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
     CK(palloc(&feat, (size_t)M, st));
@@ -349,7 +565,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     CK(palloc(&soff, (size_t)M + 1, st));
     CK(palloc(&flag, (size_t)M, st));
     CK(cudaMemsetAsync(flag, 0, (size_t)M, st));
-    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
+    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
     launch_features(Ad, Bd, feat, nullptr, h->nsm, st);
     launch_capacity(model->params, feat, ri.prod, M, B->N, model->margin, cap, h->nsm, st);
     launch_scan64(cap, soff, M, &ctl->nnz, scan_tmp, st);  // nnz field holds the slot total for now
@@ -374,7 +590,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     CK(palloc(&crp, (size_t)M + 1, st));
     if (stats) cudaEventRecord(h->ev[3], st);
     // structure (+ values of warp-sized rows) into the slots; exact counts found here
-    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag}, win, win_cap, ctl,
+    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M}, win, win_cap, ctl,
                      o.arith, h->nsm, st);
     launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
     // exact nnz(C): rows that overflowed their slot can make it larger than the slot total
@@ -393,7 +609,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     CK(palloc(&ccol, (size_t)hc.nnz, st));
     CK(palloc(&cval, (size_t)hc.nnz, st));
     launch_compact(M, soff, crp, flag, scol, sval, ccol, cval, h->nsm, st);
-    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag}, win, win_cap, ctl,
+    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag, 0, M}, win, win_cap, ctl,
                      o.arith, h->nsm, st);
     if (stats) cudaEventRecord(h->ev[4], st);
     launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, flag, scol, soff, ctl, o.arith, h->nsm, st);
@@ -440,8 +656,9 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         stats->ms_numeric = t;
         cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
         stats->ms_total = t;
-        // tiles 5, bounds 1, features 1, capacity 1, scan 3, structure 3, scan 3, compact 1, redo 3, numeric 1
-        stats->launches = (o.validate ? 2 : 0) + 22;
+        // tiles 5, bounds + binning 6, features 1, capacity 1, scan 3, structure 3, scan 3, compact 1, redo 3,
+        // numeric 1
+        stats->launches = (o.validate ? 2 : 0) + 27;
     }
 done:
     pfree(ctl, st);
@@ -453,6 +670,8 @@ done:
     pfree(ri.tmin, st);
     pfree(ri.tmax, st);
     pfree(ri.bins, st);
+    pfree(ri.cls, st);
+    pfree(ri.bin_cnt, st);
     pfree(ri.cnnz, st);
     pfree(scan_tmp, st);
     pfree(feat, st);
@@ -477,6 +696,7 @@ int row_nnz_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, int32_t
     Ctl *ctl = nullptr;
     hsmu_btiles bt{};
     RowInfo ri{};
+    int *scan_tmp = nullptr;
     DevCSR Ad = dev(A), Bd = dev(B);
     DevTiles Btd{};
     CK(palloc(&ctl, 1, st));
@@ -488,8 +708,11 @@ int row_nnz_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, int32_t
     CK(palloc(&ri.tmin, (size_t)M, st));
     CK(palloc(&ri.tmax, (size_t)M, st));
     CK(palloc(&ri.bins, (size_t)M * NBIN, st));
+    CK(palloc(&ri.cls, (size_t)M, st));
+    CK(palloc(&ri.bin_cnt, bin_scratch_ints(M), st));
+    CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
     ri.cnnz = nnz_out;
-    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), st);
+    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
     launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -505,6 +728,9 @@ done:
     pfree(ri.tmin, st);
     pfree(ri.tmax, st);
     pfree(ri.bins, st);
+    pfree(ri.cls, st);
+    pfree(ri.bin_cnt, st);
+    pfree(scan_tmp, st);
     if (rc != HSMU_OK) cudaStreamSynchronize(st);
     return rc;
 }
@@ -537,6 +763,14 @@ int hsmu_handle_create(hsmu_handle *out) {
         return HSMU_ERR_ALLOC;
     }
     for (auto &e : h->ev) cudaEventCreate(&e);
+    if (cudaStreamCreateWithFlags(&h->cs_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->cs_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+        hsmu_handle_destroy(h);
+        return HSMU_ERR_CUDA;
+    }
     // keep freed pool memory cached between calls (no re-mapping of large outputs)
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
@@ -558,6 +792,10 @@ int hsmu_handle_destroy(hsmu_handle h) {
     if (!h) return HSMU_OK;
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t s : {h->cs_in, h->cs_out})
+        if (s) cudaStreamDestroy(s);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
     delete h;
     return HSMU_OK;
@@ -566,6 +804,11 @@ int hsmu_handle_destroy(hsmu_handle h) {
 int hsmu_spgemm(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_opts *opts,
                 void *stream, hsmu_stats *stats) {
     return spgemm_impl(h, A, B, nullptr, C, opts, static_cast<cudaStream_t>(stream), stats);
+}
+
+int hsmu_spgemm_host(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_opts *opts,
+                     void *stream, hsmu_stats *stats) {
+    return spgemm_host_impl(h, A, B, C, opts, static_cast<cudaStream_t>(stream), stats);
 }
 
 int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, const hsmu_btiles *Bt, hsmu_csr *C,

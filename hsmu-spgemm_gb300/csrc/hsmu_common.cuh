@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <climits>
+
 namespace hsmu {
 
 constexpr int WARP = 32;
@@ -59,6 +61,10 @@ struct Window {
     int redo;  // 1 when emitted by the redo pass of the learned path
 };
 
+// warp-class rows with at most this many entries get their values in the
+// fused structure kernel; wider ones go through numeric windows
+constexpr int FUSE_CAP = 512;
+
 struct Ctl {
     unsigned long long products;     // sum of intermediate products
     unsigned long long win_bound;    // upper bound on the number of windows
@@ -69,7 +75,8 @@ struct Ctl {
     int err;
     int ntiles;                      // B tiles (after the B conversion scan)
     int fallback;                    // learned path: rows that did not fit their slot
-    int pad;
+    int wide_rows;                   // warp-class rows with more than FUSE_CAP entries (need windows)
+    long long binned;                // rows in the bins (total of the bin scan)
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -137,5 +144,35 @@ __device__ __forceinline__ int gallop_gt(const int *__restrict__ a, int lo, int 
 }
 
 __device__ __forceinline__ void set_err(int *err, int bit) { atomicOr(err, bit); }
+
+// OR of a 64-bit mask into shared memory as 32-bit atomics on its halves.
+// The SM executes 32-bit shared atomics natively; the 64-bit form measured
+// 2-4x slower on GB300 when lanes of a warp hit the same word.
+__device__ __forceinline__ void smem_or64(unsigned long long *p, unsigned long long v) {
+    unsigned *q = reinterpret_cast<unsigned *>(p);
+    const unsigned lo = (unsigned)v, hi = (unsigned)(v >> 32);
+    if (lo) atomicOr(q, lo);
+    if (hi) atomicOr(q + 1, hi);
+}
+
+// set bit b (0..63) of a 64-bit shared word: one 32-bit atomic
+__device__ __forceinline__ void smem_setbit64(unsigned long long *p, int b) {
+    atomicOr(reinterpret_cast<unsigned *>(p) + (b >> 5), 1u << (b & 31));
+}
+
+// Lanes hold keys in non-decreasing lane order (runs of equal keys) and a
+// 64-bit value each; returns, on the first lane of every run, the OR over
+// the run (other lanes: partial values).  Invalid lanes must carry a key
+// that no valid lane has.
+__device__ __forceinline__ unsigned long long warp_run_or(int key, unsigned long long v) {
+    const int lane = threadIdx.x & (WARP - 1);
+#pragma unroll
+    for (int d = 1; d < WARP; d <<= 1) {
+        const unsigned long long o = __shfl_down_sync(FULL, v, d);
+        const int k = __shfl_down_sync(FULL, key, d);
+        if (lane + d < WARP && k == key) v |= o;
+    }
+    return v;
+}
 
 }  // namespace hsmu

@@ -35,6 +35,7 @@ struct RowOut {
     double *cval;           // destination values
     int *cnnz;              // SPEC: exact nnz found per row
     unsigned char *flag;    // SPEC: written; REDO: rows flagged ROW_OVERFLOW are redone
+    int lo, hi;             // only rows lo <= i < hi are written (a row panel; 0, M: all rows)
 };
 
 // per-row data of A produced by the bounds kernel
@@ -42,9 +43,15 @@ struct RowInfo {
     long long *prod;   // intermediate products of the row
     int *tmin;         // first C tile id (INT_MAX for an empty row)
     int *tmax;         // last C tile id (-1 for an empty row)
-    int *bins;         // NBIN slabs of M row ids
+    int *bins;         // NBIN slabs of M row ids, each in ascending row order
     int *cnnz;         // exact nnz per row (count pass)
+    signed char *cls;  // row class (RowBin) of every row, -1 for an empty row
+    int *bin_cnt;      // [NBIN][ceil(M/32)] rows of each class per 32-row chunk, then
+                       // its exclusive scan (bin_scratch_ints(M) entries)
 };
+
+// scratch ints of RowInfo::bin_cnt for M rows
+size_t bin_scratch_ints(int M);
 
 // k_tiles.cu
 void launch_tiles_count(const DevCSR &B, int *tcnt, int validate, Ctl *ctl, int grid, cudaStream_t st);
@@ -53,7 +60,7 @@ void launch_tiles_fill(const DevCSR &B, const int *tptr, int *tcol, unsigned lon
 void launch_validate(const DevCSR &A, Ctl *ctl, int grid, cudaStream_t st);
 
 // k_rows.cu
-void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int grid,
+void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int grid, int *scan_tmp,
                    cudaStream_t st);
 // exclusive scan of int counts (n entries) into out[0..n]; total (int64) into *total64;
 // sets DERR_OVERFLOW if the total exceeds INT32_MAX.  tmp must hold scan_tmp_ints(n) ints.

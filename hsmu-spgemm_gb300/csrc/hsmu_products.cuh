@@ -3,8 +3,10 @@
 // accumulator for one C row (or one window of it), in the oracle's order.
 //
 // Order: for each C entry the products are added as 0.0 + p_1 + p_2 + ...
-// in A(i,:)'s storage order; each p = a*b is rounded first (no FMA), exactly
-// like the host Gustavson oracle, so results are bit-identical to it.
+// in A(i,:)'s storage order, exactly like the host Gustavson oracle, so
+// results are bit-identical to it in each arithmetic mode (AR_RN: every
+// p = a*b rounded before the add, as the reference does; AR_FMA: each step
+// one fused multiply-add).
 //
 // The A entries are taken 32 at a time (one per lane); seg(p) gives the B
 // entry range [elo, ehi) that A entry p contributes to this accumulator.
@@ -22,15 +24,31 @@
 
 namespace hsmu {
 
-template <bool INT_MUL>
-__device__ __forceinline__ double prod_mul(double a, double b) {
-    if (INT_MUL) return dmul_int(a, b);
+// Arithmetic of one accumulation step c <- c + a*b (hsmu_opts.arith):
+//   AR_RN   (0) product rounded, then added: RN(c + RN(a*b));
+//   AR_FMA  (1) fused, one rounding per product: RN(c + a*b) -- one FP64
+//               pipe operation per product instead of two;
+//   AR_IMUL (2) as AR_RN, with the product formed exactly on the integer pipe.
+// term() is what can be computed before the accumulator slot is known;
+// add_term() folds it into the accumulator.
+enum Arith { AR_RN = 0, AR_FMA = 1, AR_IMUL = 2 };
+
+template <int AR>
+__device__ __forceinline__ double term(double a, double b) {
+    if (AR == AR_FMA) return b;
+    if (AR == AR_IMUL) return dmul_int(a, b);
     return __dmul_rn(a, b);
+}
+
+template <int AR>
+__device__ __forceinline__ double add_term(double c, double a, double t) {
+    if (AR == AR_FMA) return __fma_rn(a, t, c);
+    return __dadd_rn(c, t);
 }
 
 // SegFn:    void(int p, int k, int &elo, int &ehi)  -- called for valid lanes
 // LookupFn: int(int j) -> slot in acc, or -1 if j is not in the accumulator
-template <bool INT_MUL, bool NC = true, class SegFn, class LookupFn>
+template <int AR, bool NC = true, class SegFn, class LookupFn>
 __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *__restrict__ acol,
                                                 const double *__restrict__ aval, const int *__restrict__ brp,
                                                 const int *__restrict__ bcol, const double *__restrict__ bval,
@@ -87,9 +105,9 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
                     b1 = ldx<NC>(bval + n_es + n_off + lane);
                 }
                 if (off + lane < ls) {
-                    const double pr = prod_mul<INT_MUL>(as, b0);
+                    const double pr = term<AR>(as, b0);
                     const int q = lookup(j0);
-                    if (q >= 0) acc[q] = __dadd_rn(acc[q], pr);
+                    if (q >= 0) acc[q] = add_term<AR>(acc[q], as, pr);
                     else bad = true;
                 }
                 if (!have_next) break;
@@ -133,7 +151,7 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
             int slot = -1 - lane;
             double pr = 0.0;
             if (gv) {
-                pr = prod_mul<INT_MUL>(as, b);
+                pr = term<AR>(as, b);
                 const int q = lookup(j);
                 if (q >= 0) slot = q;
                 else bad = true;
@@ -143,16 +161,16 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
             const int smax = (int)__reduce_max_sync(FULL, act ? (unsigned)sg : 0u);
             if (smin >= smax) {
                 // one A entry in this step: all slots distinct
-                if (act) acc[slot] = __dadd_rn(acc[slot], pr);
+                if (act) acc[slot] = add_term<AR>(acc[slot], as, pr);
             } else {
                 const unsigned grp = __match_any_sync(FULL, slot);
                 const int rank = __popc(grp & lanemask_lt());
                 const int maxr = (int)__reduce_max_sync(FULL, act ? (unsigned)rank : 0u);
                 for (int rr = 0; rr < maxr; rr++) {
-                    if (act && rank == rr) acc[slot] = __dadd_rn(acc[slot], pr);
+                    if (act && rank == rr) acc[slot] = add_term<AR>(acc[slot], as, pr);
                     __syncwarp();
                 }
-                if (act && rank == maxr) acc[slot] = __dadd_rn(acc[slot], pr);
+                if (act && rank == maxr) acc[slot] = add_term<AR>(acc[slot], as, pr);
             }
             __syncwarp();
             sg = sg_n;

@@ -7,13 +7,14 @@
 // oracle's order (A entry, then B entry), keeping the distinct columns in a
 // small sorted list (insertion), so the count pass and the fill pass need no
 // B tiles and no sorting afterwards.  In the fill pass every product is added
-// to its column's accumulator in that same order: 0.0 + p_1 + p_2 + ...,
-// each p rounded before the add, bit-identical to the host oracle.
+// to its column's accumulator in that same order: 0.0 + p_1 + p_2 + ...
+// (arithmetic per step as in hsmu_products.cuh), bit-identical to the host
+// oracle.
 //
 // The per-thread lists live in shared memory laid out element-major
 // ([TINY_MAX][threads]) so that neighbouring threads hit neighbouring banks.
 #pragma once
-#include "hsmu_common.cuh"
+#include "hsmu_products.cuh"
 
 namespace hsmu {
 
@@ -46,12 +47,12 @@ __device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__r
 // Fills the row's sorted columns and values at out_col/out_val and returns
 // its nnz; returns -1 on an inconsistency (more than TINY_MAX products, or
 // more than `cap` distinct columns).
-template <bool NC = true, class MulFn>
+template <int AR, bool NC = true>
 __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
                                              const double *__restrict__ aval, const int *__restrict__ brp,
                                              const int *__restrict__ bcol, const double *__restrict__ bval,
                                              int *cols, double *acc, int stride, int cap, int *__restrict__ out_col,
-                                             double *__restrict__ out_val, MulFn mul) {
+                                             double *__restrict__ out_val) {
     int n = 0, seen = 0;
     for (int p = a_lo; p < a_hi; p++) {
         const int k = ldx<NC>(acol + p);
@@ -60,11 +61,11 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
         for (int q = ldx<NC>(brp + k); q < qe; q++) {
             if (++seen > TINY_MAX) return -1;
             const int j = ldx<NC>(bcol + q);
-            const double pr = mul(a, ldx<NC>(bval + q));
+            const double pr = term<AR>(a, ldx<NC>(bval + q));
             int pos = n;
             while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
             if (pos > 0 && cols[(pos - 1) * stride] == j) {
-                acc[(pos - 1) * stride] = __dadd_rn(acc[(pos - 1) * stride], pr);
+                acc[(pos - 1) * stride] = add_term<AR>(acc[(pos - 1) * stride], a, pr);
                 continue;
             }
             for (int t = n; t > pos; t--) {
@@ -72,7 +73,7 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
                 acc[t * stride] = acc[(t - 1) * stride];
             }
             cols[pos * stride] = j;
-            acc[pos * stride] = __dadd_rn(0.0, pr);
+            acc[pos * stride] = add_term<AR>(0.0, a, pr);
             n++;
         }
     }
@@ -84,12 +85,6 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
     return n;
 }
 
-}  // namespace hsmu
-
-#include "hsmu_block.cuh"
-#include "hsmu_products.cuh"
-
-namespace hsmu {
 
 // ---------------------------------------------------------------------------
 // Warp-per-row routines on a dense span table, driven by B's entries (no B
@@ -134,7 +129,7 @@ __device__ __forceinline__ bool warp_row_masks(int a_lo, int a_hi, const int *__
     warp_walk_tiles<false, NC>(a_lo, a_hi, 0, WARP, acol, brp, bcol, 0, 0, [&](int q) {
         const int j = ldx<NC>(bcol + q);
         const int t = (j >> 6) - t0;
-        if (t >= 0 && t < span) atomicOr(msk + t, 1ull << (j & 63));
+        if (t >= 0 && t < span) smem_setbit64(msk + t, j & 63);
         else bad = true;
     });
     __syncwarp();
@@ -151,7 +146,7 @@ __device__ __forceinline__ int warp_mask_count(const unsigned long long *msk, in
 // Given the row's masks: write its sorted columns to out_col, accumulate the
 // products (oracle order) in acc and write the values to out_val.  nnz must
 // equal the masks' popcount and be <= cap.  Returns false on inconsistency.
-template <bool INT_MUL, bool NC = true>
+template <int AR, bool NC = true>
 __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
                                               const double *__restrict__ aval, const int *__restrict__ brp,
                                               const int *__restrict__ bcol, const double *__restrict__ bval,
@@ -192,7 +187,7 @@ __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__r
         return base[t] + rank64(m, bit);
     };
     bool bad = false;
-    warp_accumulate<INT_MUL, NC>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, acc, bad);
+    warp_accumulate<AR, NC>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, acc, bad);
     __syncwarp();
     for (int q = lane; q < nnz; q += WARP) out_val[q] = acc[q];
     __syncwarp();

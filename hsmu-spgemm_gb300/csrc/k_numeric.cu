@@ -54,7 +54,7 @@ static_assert(WIN_OCCW == 2 * WARP, "prefix pass assumes two occupancy words per
 __device__ __forceinline__ unsigned lanemask_le() { return lanemask_lt() | (1u << lane_id()); }
 
 
-template <bool INT_MUL>
+template <int AR>
 __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(const int *__restrict__ arp, const int *__restrict__ acol,
                                                             const double *__restrict__ aval,
                                                             const int *__restrict__ brp, const int *__restrict__ bcol,
@@ -125,24 +125,28 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                     const int c = v ? src[s] : 0;
                     if (v && from_slot) ccol[s0 + s] = c;
                     const int t = (c >> 6) - t0;
-                    int tp = __shfl_up_sync(FULL, t, 1);
-                    if (lane == 0) tp = prev_t;
+                    const int t_up = __shfl_up_sync(FULL, t, 1);
+                    const int tp = lane == 0 ? prev_t : t_up;
                     const bool head = v && t != tp;
                     const unsigned heads = __ballot_sync(FULL, head);
                     const int rank = dense ? t : run + __popc(heads & lanemask_le()) - 1;
+                    // columns are sorted: lanes of one tile are a run; its first lane stores the OR
+                    const unsigned long long bits = warp_run_or(v ? t : INT_MAX, v ? 1ull << (c & 63) : 0ull);
+                    const bool first_of_run = v && (lane == 0 || t != t_up);
                     if (v) {
                         if (t < 0 || t >= span || rank < 0 || rank >= WIN_TCAP) {
                             bad = true;
                         } else {
                             if (head) {
                                 S.tbase[rank] = s;
-                                if (!dense) atomicOr(&S.occ[t >> 6], 1ull << (t & 63));
+                                if (!dense) smem_setbit64(&S.occ[t >> 6], t & 63);
                             }
-                            atomicOr(&S.tmask[rank], 1ull << (c & 63));
+                            if (first_of_run) S.tmask[rank] |= bits;
                         }
                     }
                     run += __popc(heads);
                     prev_t = __shfl_sync(FULL, t, min(WARP, cnt - sb) - 1);
+                    __syncwarp();
                 }
             }
             __syncwarp();
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 ehi = last ? be : gallop_gt(bcol, elo, be, c_hi);
                 if (keep) S.cur[p - a_lo] = ehi;
             };
-            warp_accumulate<INT_MUL>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
+            warp_accumulate<AR>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
             __syncwarp();
             for (int q = lane; q < cnt; q += WARP) cval[s0 + q] = S.acc[q];
             __syncwarp();
@@ -194,17 +198,18 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
 void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
                     const long long *soff, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
-    auto k = arith == 2 ? k_numeric<true> : k_numeric<false>;
+    auto k = arith == AR_IMUL ? k_numeric<AR_IMUL> : arith == AR_FMA ? k_numeric<AR_FMA> : k_numeric<AR_RN>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
         A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, ctl);
 }
 
 int configure_numeric() {
-    int e = (int)cudaFuncSetAttribute(k_numeric<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      NUM_WARPS * (int)sizeof(NumSmem));
-    if (e) return e;
-    return (int)cudaFuncSetAttribute(k_numeric<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     NUM_WARPS * (int)sizeof(NumSmem));
+    for (auto k : {k_numeric<AR_RN>, k_numeric<AR_FMA>, k_numeric<AR_IMUL>}) {
+        const int e = (int)cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                NUM_WARPS * (int)sizeof(NumSmem));
+        if (e) return e;
+    }
+    return 0;
 }
 
 // self-test of the integer-pipe multiply against the FP64 pipe on n operand

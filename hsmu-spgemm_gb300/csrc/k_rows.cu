@@ -8,7 +8,9 @@
 // the ends of B's sorted tile lists).  The tile span decides the row class
 // (one warp with a dense span table, or one CTA with a chunked table), which
 // replaces the reference's host-round-trip binning (src/bining.cuh:1-207):
-// rows are binned on the device with block-aggregated atomics.
+// rows are binned on the device by a stable compaction (count per 32-row
+// chunk, scan, emit), so every bin lists its rows in ascending order and the
+// rows of a row panel are one contiguous slice of each bin.
 //
 // Scan: three launches (block sums, scan of block sums, block scans), 64-bit
 // running totals, int32 output; replaces cub::DeviceScan::ExclusiveSum plus
@@ -28,7 +30,6 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                                                 const int *__restrict__ tcol, int N, RowInfo ri, Ctl *ctl) {
     constexpr int RPB = 256 / G;  // rows per block iteration
     __shared__ int s_cnt[NBIN];
-    __shared__ int s_base[NBIN];
     const int sub = threadIdx.x & (G - 1);
     const int rloc = threadIdx.x / G;
     unsigned long long my_prod = 0, my_wb = 0;
@@ -55,33 +56,28 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
             tmin = min(tmin, __shfl_xor_sync(FULL, tmin, d, G));
             tmax = max(tmax, __shfl_xor_sync(FULL, tmax, d, G));
         }
-        int bin = -1, lpos = 0;
         if (i < M && sub == 0) {
             ri.prod[i] = prod;
             ri.tmin[i] = tmin;
             ri.tmax[i] = tmax;
+            int bin = -1;
             if (prod == 0) {
                 ri.cnnz[i] = 0;
             } else {
                 const int span = tmax - tmin + 1;
                 bin = prod <= TINY_MAX ? BIN_TINY : (span <= SPAN_T ? BIN_DS : BIN_L);
-                lpos = atomicAdd(&s_cnt[bin], 1);
+                atomicAdd(&s_cnt[bin], 1);
                 my_prod += (unsigned long long)prod;
                 const long long cap = prod < (long long)N ? prod : (long long)N;
                 // windows per row <= slot cuts + tile-rank cuts + span cuts + 1
                 const long long tl = cap < (long long)span ? cap : (long long)span;
                 my_wb += (unsigned long long)(cap / WIN_CUT + tl / WIN_TCAP + (span - 1) / WIN_SPAN + 1);
             }
+            ri.cls[i] = (signed char)bin;
         }
-        __syncthreads();
-        if (threadIdx.x < NBIN) {
-            s_base[threadIdx.x] = s_cnt[threadIdx.x] ? atomicAdd(&ctl->bin_count[threadIdx.x], s_cnt[threadIdx.x]) : 0;
-            s_cnt[threadIdx.x] = 0;
-        }
-        __syncthreads();
-        if (bin >= 0) ri.bins[(size_t)bin * M + s_base[bin] + lpos] = i;
-        __syncthreads();
     }
+    __syncthreads();
+    if (threadIdx.x < NBIN && s_cnt[threadIdx.x]) atomicAdd(&ctl->bin_count[threadIdx.x], s_cnt[threadIdx.x]);
     my_prod = warp_sum(my_prod);
     my_wb = warp_sum(my_wb);
     if (lane_id() == 0) {
@@ -90,8 +86,41 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     }
 }
 
+// stable binning: rows of each class per 32-row chunk (warp per chunk) ...
+__global__ void __launch_bounds__(256) k_bin_count(int M, const signed char *__restrict__ cls, int *__restrict__ cnt) {
+    const int nch = (M + WARP - 1) / WARP;
+    const int lane = lane_id();
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) / WARP; c < nch; c += gridDim.x * blockDim.x / WARP) {
+        const int i = c * WARP + lane;
+        const int b = i < M ? cls[i] : -1;
+#pragma unroll
+        for (int k = 0; k < NBIN; k++) {
+            const int n = __popc(__ballot_sync(FULL, b == k));
+            if (lane == k) cnt[k * nch + c] = n;
+        }
+    }
+}
+
+// ... then, after the scan of those counts, every row at its place in its bin
+__global__ void __launch_bounds__(256) k_bin_emit(int M, const signed char *__restrict__ cls,
+                                                  const int *__restrict__ off, int *__restrict__ bins) {
+    const int nch = (M + WARP - 1) / WARP;
+    const int lane = lane_id();
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) / WARP; c < nch; c += gridDim.x * blockDim.x / WARP) {
+        const int i = c * WARP + lane;
+        const int b = i < M ? cls[i] : -1;
+#pragma unroll
+        for (int k = 0; k < NBIN; k++) {
+            const unsigned m = __ballot_sync(FULL, b == k);
+            if (b == k) bins[(size_t)k * M + (off[k * nch + c] - off[k * nch]) + __popc(m & lanemask_lt())] = i;
+        }
+    }
+}
+
+size_t bin_scratch_ints(int M) { return (size_t)NBIN * ((M + WARP - 1) / WARP) * 2 + 2; }
+
 void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int grid,
-                   cudaStream_t st) {
+                   int *scan_tmp, cudaStream_t st) {
     const double avg = A.M ? (double)A.nnz / A.M : 0.0;
     if (avg <= 6)
         k_bounds<4><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
@@ -101,6 +130,11 @@ void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo
         k_bounds<16><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
     else
         k_bounds<32><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+    const int nch = (A.M + WARP - 1) / WARP;
+    int *cnt = ri.bin_cnt, *off = ri.bin_cnt + (size_t)NBIN * nch + 1;
+    k_bin_count<<<grid, 256, 0, st>>>(A.M, ri.cls, cnt);
+    launch_scan(cnt, off, NBIN * nch, &ctl->binned, scan_tmp, ctl, st);
+    k_bin_emit<<<grid, 256, 0, st>>>(A.M, ri.cls, off, ri.bins);
 }
 
 // ---------------------------------------------------------------- scan

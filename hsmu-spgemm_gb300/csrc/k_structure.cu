@@ -36,6 +36,17 @@
 
 namespace hsmu {
 
+// positions [b0, b1) of a bin (rows in ascending order) that hold the panel's rows lo <= i < hi
+__device__ __forceinline__ void bin_slice(const int *rows, int n, const RowOut &o, int M, int &b0, int &b1) {
+    b0 = o.lo > 0 ? lower_bound_i32(rows, 0, n, o.lo) : 0;
+    b1 = o.hi < M ? lower_bound_i32(rows, b0, n, o.hi) : n;
+}
+
+// rows outside the panel, and in REDO mode rows that fitted their slots, are left alone
+__device__ __forceinline__ bool skip_row(const RowOut &o, int i) {
+    return i < o.lo || i >= o.hi || (o.mode == OUT_REDO && o.flag[i] != ROW_OVERFLOW);
+}
+
 __device__ __forceinline__ long long out_base(const RowOut &o, int i) {
     return o.mode == OUT_SPEC ? o.soff[i] : (long long)o.crp[i];
 }
@@ -46,7 +57,6 @@ __device__ __forceinline__ int out_limit(const RowOut &o, int i) {
 constexpr int SDS_WARPS = 4;
 constexpr int SDS_CTAS_PER_SM = 5;
 constexpr int SDS_WL = 64;     // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
-constexpr int FUSE_CAP = 512;  // rows up to this many entries get their values here
 
 struct SdsSmem {
     unsigned long long msk[SPAN_T];
@@ -56,7 +66,7 @@ struct SdsSmem {
     double acc[FUSE_CAP];
 };
 
-template <bool INT_MUL>
+template <int AR>
 __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
     k_struct_ds(int M, const int *__restrict__ arp, const int *__restrict__ acol, const double *__restrict__ aval,
                 const int *__restrict__ brp, const int *__restrict__ bcol, const double *__restrict__ bval,
@@ -66,13 +76,14 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
     extern __shared__ unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     SdsSmem &S = reinterpret_cast<SdsSmem *>(s_dyn)[w];
-    const int n = ctl->bin_count[BIN_DS];
     const int *rows = ri.bins + (size_t)BIN_DS * M;
+    int b0, b1;
+    bin_slice(rows, ctl->bin_count[BIN_DS], out, M, b0, b1);
     int *__restrict__ ccol = out.ccol;
     double *__restrict__ cval = out.cval;
-    for (int r = blockIdx.x * SDS_WARPS + w; r < n; r += gridDim.x * SDS_WARPS) {
+    for (int r = b0 + blockIdx.x * SDS_WARPS + w; r < b1; r += gridDim.x * SDS_WARPS) {
         const int i = rows[r];
-        if (out.mode == OUT_REDO && out.flag[i] != ROW_OVERFLOW) continue;
+        if (skip_row(out, i)) continue;
         const int t0 = ri.tmin[i];
         const int span = ri.tmax[i] - t0 + 1;
         const long long rowbase = out_base(out, i);
@@ -82,7 +93,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
         bool bad = false;
         warp_walk_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, 0, 0, [&](int idx) {
             const int t = __ldg(tcol + idx) - t0;
-            if (t >= 0 && t < span) atomicOr(&S.msk[t], __ldg(tmask + idx));
+            if (t >= 0 && t < span) smem_or64(&S.msk[t], __ldg(tmask + idx));
             else bad = true;
         });
         if (__any_sync(FULL, bad)) {
@@ -157,7 +168,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
                 return S.base[t] + rank64(m, bit);
             };
             bool vbad = false;
-            warp_accumulate<INT_MUL>(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, seg, lookup, S.acc, vbad);
+            warp_accumulate<AR>(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, seg, lookup, S.acc, vbad);
             __syncwarp();
             for (int q = lane; q < nnz; q += WARP) cval[rowbase + q] = S.acc[q];
             if (__any_sync(FULL, vbad) && lane == 0) set_err(&ctl->err, DERR_INTERNAL);
@@ -252,12 +263,13 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
     __shared__ int s_wbase;
     constexpr int NWARP = SL_THREADS / 32;
     const int w = threadIdx.x >> 5;
-    const int n = ctl->bin_count[BIN_L];
     const int *rows = ri.bins + (size_t)BIN_L * M;
+    int b0, b1;
+    bin_slice(rows, ctl->bin_count[BIN_L], out, M, b0, b1);
     int *__restrict__ ccol = out.ccol;
-    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+    for (int r = b0 + blockIdx.x; r < b1; r += gridDim.x) {
         const int i = rows[r];
-        if (out.mode == OUT_REDO && out.flag[i] != ROW_OVERFLOW) continue;
+        if (skip_row(out, i)) continue;
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
         const int a_lo = arp[i], a_hi = arp[i + 1];
         const long long rowbase = out_base(out, i);
@@ -272,7 +284,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             bool bad = false;
             auto orfn = [&](int idx) {
                 const int t = __ldg(tcol + idx) - c0;
-                if (t >= 0 && t < len) atomicOr(&S.msk[t], __ldg(tmask + idx));
+                if (t >= 0 && t < len) smem_or64(&S.msk[t], __ldg(tmask + idx));
                 else bad = true;
             };
             if (one_chunk)
@@ -381,7 +393,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
 constexpr int TINYF_THREADS = 128;
 
 // tiny rows: one thread per row writes its sorted columns and values
-template <bool INT_MUL>
+template <int AR>
 __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *__restrict__ arp,
                                                              const int *__restrict__ acol,
                                                              const double *__restrict__ aval,
@@ -391,17 +403,17 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
                                                              RowOut out, Ctl *ctl) {
     __shared__ int s_cols[TINY_MAX * TINYF_THREADS];
     __shared__ double s_acc[TINY_MAX * TINYF_THREADS];
-    const int n = ctl->bin_count[BIN_TINY];
     const int *rows = ri.bins + (size_t)BIN_TINY * M;
+    int b0, b1;
+    bin_slice(rows, ctl->bin_count[BIN_TINY], out, M, b0, b1);
     bool bad = false;
-    for (int r = blockIdx.x * TINYF_THREADS + threadIdx.x; r < n; r += gridDim.x * TINYF_THREADS) {
+    for (int r = b0 + blockIdx.x * TINYF_THREADS + threadIdx.x; r < b1; r += gridDim.x * TINYF_THREADS) {
         const int i = rows[r];
-        if (out.mode == OUT_REDO && out.flag[i] != ROW_OVERFLOW) continue;
+        if (skip_row(out, i)) continue;
         const long long c0 = out_base(out, i);
         const int lim = out_limit(out, i);
-        const int got = tiny_row_fill(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, s_cols + threadIdx.x,
-                                      s_acc + threadIdx.x, TINYF_THREADS, lim, out.ccol + c0, out.cval + c0,
-                                      [](double x, double y) { return prod_mul<INT_MUL>(x, y); });
+        const int got = tiny_row_fill<AR>(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, s_cols + threadIdx.x,
+                                          s_acc + threadIdx.x, TINYF_THREADS, lim, out.ccol + c0, out.cval + c0);
         if (out.mode == OUT_SPEC) {
             out.cnnz[i] = got < 0 ? 0 : got;
             out.flag[i] = got < 0 ? ROW_OVERFLOW : ROW_VALUES;
@@ -415,9 +427,9 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
 
 void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
                       long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
-    auto kt = arith == 2 ? k_fill_tiny<true> : k_fill_tiny<false>;
+    auto kt = arith == AR_IMUL ? k_fill_tiny<AR_IMUL> : arith == AR_FMA ? k_fill_tiny<AR_FMA> : k_fill_tiny<AR_RN>;
     kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, out, ctl);
-    auto kds = arith == 2 ? k_struct_ds<true> : k_struct_ds<false>;
+    auto kds = arith == AR_IMUL ? k_struct_ds<AR_IMUL> : arith == AR_FMA ? k_struct_ds<AR_FMA> : k_struct_ds<AR_RN>;
     kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
         A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
     k_struct_l<<<nsm * 2, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
@@ -425,12 +437,11 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
 }
 
 int configure_structure() {
-    int e = (int)cudaFuncSetAttribute(k_struct_ds<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SDS_WARPS * (int)sizeof(SdsSmem));
-    if (e) return e;
-    e = (int)cudaFuncSetAttribute(k_struct_ds<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  SDS_WARPS * (int)sizeof(SdsSmem));
-    if (e) return e;
+    for (auto k : {k_struct_ds<AR_RN>, k_struct_ds<AR_FMA>, k_struct_ds<AR_IMUL>}) {
+        const int e = (int)cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                SDS_WARPS * (int)sizeof(SdsSmem));
+        if (e) return e;
+    }
     return (int)cudaFuncSetAttribute(k_struct_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SlSmem));
 }
 

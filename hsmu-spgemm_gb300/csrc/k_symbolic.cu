@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
         bool bad = false;
         warp_walk_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, 0, 0, [&](int idx) {
             const int t = __ldg(tcol + idx) - t0;
-            if (t >= 0 && t < span) atomicOr(msk + t, __ldg(tmask + idx));
+            if (t >= 0 && t < span) smem_or64(msk + t, __ldg(tmask + idx));
             else bad = true;
         });
         if (bad) set_err(&ctl->err, DERR_INTERNAL);
@@ -50,7 +50,10 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
         int cnt = 0;
         for (int t = lane; t < span; t += WARP) cnt += popc64(msk[t]);
         cnt = warp_sum(cnt);
-        if (lane == 0) ri.cnnz[i] = cnt;
+        if (lane == 0) {
+            ri.cnnz[i] = cnt;
+            if (cnt > FUSE_CAP) atomicAdd(&ctl->wide_rows, 1);
+        }
         __syncwarp();
     }
 }
@@ -83,7 +86,7 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
             bool bad = false;
             auto orfn = [&](int idx) {
                 const int t = __ldg(tcol + idx) - c0;
-                if (t >= 0 && t < c1 - c0) atomicOr(msk + t, __ldg(tmask + idx));
+                if (t >= 0 && t < c1 - c0) smem_or64(msk + t, __ldg(tmask + idx));
                 else bad = true;
             };
             if (one_chunk)

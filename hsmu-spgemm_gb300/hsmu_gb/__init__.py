@@ -29,12 +29,15 @@ LIB_PATH = os.path.join(PKG, "libhsmu_gb.so")
 HSMU_OK = 0
 STATUS = {0: "HSMU_OK", 1: "HSMU_ERR_INVALID", 2: "HSMU_ERR_ALLOC", 3: "HSMU_ERR_CUDA",
           4: "HSMU_ERR_OVERFLOW", 5: "HSMU_ERR_UNSORTED", 6: "HSMU_ERR_INTERNAL",
-          7: "HSMU_ERR_TIMEOUT", 8: "HSMU_ERR_NO_DEVICE", 9: "HSMU_ERR_UNSUPPORTED"}
+          7: "HSMU_ERR_TIMEOUT", 8: "HSMU_ERR_NO_DEVICE", 9: "HSMU_ERR_UNSUPPORTED",
+          10: "HSMU_ERR_CAPACITY"}
+HSMU_ERR_CAPACITY = 10
 BATCH_PRODUCT, BATCH_GALERKIN = 0, 1
+ARITH_RN, ARITH_FMA, ARITH_IMUL = 0, 1, 2  # hsmu_opts.arith
 
 # every symbol include/hsmu_gb.h declares (checked by the CPU test suite)
 EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_handle_destroy",
-           "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_btiles_build", "hsmu_btiles_free",
+           "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_spgemm_host", "hsmu_btiles_build", "hsmu_btiles_free",
            "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul", "hsmu_btiles_build_noalloc",
            "hsmu_batch_create", "hsmu_batch_execute", "hsmu_batch_graph_launch", "hsmu_batch_status",
            "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
@@ -64,7 +67,7 @@ class c_btiles(ctypes.Structure):
 
 class c_opts(ctypes.Structure):
     _fields_ = [("validate", ctypes.c_int32), ("arith", ctypes.c_int32),
-                ("window_cap", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("window_cap", ctypes.c_int32), ("panels", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class c_mlp(ctypes.Structure):
@@ -108,6 +111,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_spgemm_tiled.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
                                     ctypes.POINTER(c_btiles), ctypes.POINTER(c_csr),
                                     ctypes.POINTER(c_opts), P, ctypes.POINTER(c_stats)]
+    L.hsmu_spgemm_host.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
+                                   ctypes.POINTER(c_opts), P, ctypes.POINTER(c_stats)]
     L.hsmu_btiles_build.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_btiles), P]
     L.hsmu_btiles_free.argtypes = [ctypes.POINTER(c_btiles)]
     L.hsmu_csr_free.argtypes = [ctypes.POINTER(c_csr)]
@@ -349,6 +354,66 @@ class Engine:
         _check(rc, "hsmu_spgemm")
         self.last_stats = st.as_dict() if stats else None
         return DeviceCSR(C)
+
+
+    def spgemm_host(self, A, B, out=None, *, arith: int = 0, panels: int = 0, validate: bool = False,
+                    stream=None, stats: bool = False):
+        """C = A * B with host operands and a host result (hsmu_spgemm_host).
+
+        A, B: objects with M, N and host arrays row_ptr (int32), col (int32),
+        val (float64) -- numpy arrays or CPU torch tensors (page-locked ones let
+        the copies overlap the compute).  out: (row_ptr, col, val) host arrays
+        to fill, col/val of any capacity; None allocates numpy arrays of the
+        exact size (one extra symbolic pass).  Returns (row_ptr, col, val) of
+        length M+1, nnz, nnz as views of the output arrays."""
+        L = load_library()
+        a = _host_desc(A)
+        b = a if B is A else _host_desc(B)
+        o = c_opts(int(validate), int(arith), 0, int(panels))
+        st = c_stats()
+        sp = ctypes.byref(st) if stats else None
+        if out is None:
+            probe = np.empty(A.M + 1, np.int32)
+            c = c_csr(A.M, B.N, 0, 0, _host_ptr(probe), None, None)
+            rc = L.hsmu_spgemm_host(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                    ctypes.byref(o), _stream_ptr(stream), None)
+            if rc not in (HSMU_OK, HSMU_ERR_CAPACITY):
+                _check(rc, "hsmu_spgemm_host")
+            out = (probe, np.empty(c.nnz, np.int32), np.empty(c.nnz, np.float64))
+        rp, col, val = out
+        cap = min(_host_len(col), _host_len(val))
+        c = c_csr(A.M, B.N, cap, 0, _host_ptr(rp), _host_ptr(col), _host_ptr(val))
+        rc = L.hsmu_spgemm_host(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(o),
+                                _stream_ptr(stream), sp)
+        _check(rc, "hsmu_spgemm_host")
+        self.last_stats = st.as_dict() if stats else None
+        return rp[:A.M + 1], col[:c.nnz], val[:c.nnz]
+
+
+def _host_ptr(x):
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        if x.is_cuda or not x.is_contiguous():
+            raise ValueError("host arrays must be contiguous CPU tensors")
+        return x.data_ptr()
+    if not x.flags["C_CONTIGUOUS"]:
+        raise ValueError("host arrays must be contiguous")
+    return x.ctypes.data
+
+
+def _host_len(x) -> int:
+    return int(x.numel()) if hasattr(x, "numel") else int(x.size)
+
+
+def _host_desc(X) -> c_csr:
+    for arr, dt in ((X.row_ptr, "int32"), (X.col, "int32"), (X.val, "float64")):
+        name = str(arr.dtype).replace("torch.", "")
+        if name != dt:
+            raise ValueError("host CSR arrays must be int32/int32/float64, got %s" % name)
+    nnz = _host_len(X.col)
+    return c_csr(X.M, X.N, nnz, 0, _host_ptr(X.row_ptr), _host_ptr(X.col) if nnz else None,
+                 _host_ptr(X.val) if nnz else None)
 
 
 class Batch:

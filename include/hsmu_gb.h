@@ -46,7 +46,8 @@ typedef enum hsmu_status {
     HSMU_ERR_INTERNAL = 6,     /* a device-side consistency check failed */
     HSMU_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up */
     HSMU_ERR_NO_DEVICE = 8,    /* no usable sm_103 device */
-    HSMU_ERR_UNSUPPORTED = 9   /* a batch holds rows that need the plain engine's large-row path */
+    HSMU_ERR_UNSUPPORTED = 9,  /* a batch holds rows that need the plain engine's large-row path */
+    HSMU_ERR_CAPACITY = 10     /* hsmu_spgemm_host: output buffers too small (C->nnz = needed size) */
 } hsmu_status;
 
 /* CSR matrix descriptor.  row_ptr has M+1 entries, col/val have nnz entries.
@@ -81,11 +82,25 @@ typedef struct hsmu_btiles {
 } hsmu_btiles;
 
 /* Options; a NULL pointer means all defaults (zero-initialise to get them). */
+#define HSMU_ARITH_RN 0
+#define HSMU_ARITH_FMA 1
+#define HSMU_ARITH_IMUL 2
 typedef struct hsmu_opts {
     int32_t validate;     /* 1: check A and B are canonical CSR before computing */
-    int32_t arith;        /* 0: FP64-pipe multiply (default), 2: exact integer-pipe multiply */
+    int32_t arith;        /* how each product is accumulated, c <- c + a*b:
+                           * HSMU_ARITH_RN (0, default): product rounded, then added -- the
+                           *   reference's arithmetic (atomicAdd(.., aval * bval),
+                           *   src/compressed/compressed_Cval.cuh:60-61);
+                           * HSMU_ARITH_FMA (1): one fused multiply-add per product (one
+                           *   rounding instead of two, half the FP64 instructions);
+                           * HSMU_ARITH_IMUL (2): as RN, with the product formed exactly on the
+                           *   integer pipe.
+                           * In every mode products are added in A-row order, so results are
+                           * deterministic; RN and IMUL give identical bits. */
     int32_t window_cap;   /* 0: default slots per numeric window (<= 4096) */
-    int32_t reserved[5];
+    int32_t panels;       /* hsmu_spgemm_host: row panels of the copy pipeline (0: one per 32 MB
+                           * of output; at most 8), sized in a decreasing geometric series */
+    int32_t reserved[4];
 } hsmu_opts;
 
 /* Per-call statistics (filled by hsmu_spgemm when stats != NULL). */
@@ -131,6 +146,26 @@ int hsmu_spgemm(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C
 int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B,
                       const hsmu_btiles *Bt, hsmu_csr *C, const hsmu_opts *opts,
                       void *stream, hsmu_stats *stats);
+
+/* C = A * B with A, B and C in HOST memory: the whole sequence a reference
+ * caller runs around NHC_spgemm -- HtD_value_col_ptr(&A), HtD_value_col_ptr(&B)
+ * (src/test.cu:67-68, src/loading.cuh:86-94), NHC_spgemm (src/test.cu:71)
+ * and the copy of C back to the host -- as one pipelined call.  The index
+ * arrays go up first and the symbolic pass starts on them while the values
+ * are copied on a second stream; C is then computed in row panels and each
+ * finished panel is copied back on a third stream while the next one is
+ * computed.  Results are identical to hsmu_spgemm + hsmu_csr_download.
+ *   A, B: host arrays; when A and B are the same arrays they are copied once.
+ *   C:    in:  row_ptr (A->M + 1 entries), col and val of capacity C->nnz;
+ *         out: M, N, nnz, and the three arrays filled; owned = 0.
+ * HSMU_ERR_CAPACITY: C->nnz < nnz(C); C->nnz and C->row_ptr then hold the
+ * product's, col/val are untouched -- call again with larger arrays.
+ * Host arrays must be page-locked (cudaHostAlloc / cudaHostRegister) for the
+ * copies to overlap; pageable memory gives the same result, serialised.
+ * Blocks until C is in host memory.  In stats, ms_structure covers the panels'
+ * kernels (with the copies they hide) and ms_numeric the last copies. */
+int hsmu_spgemm_host(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C,
+                     const hsmu_opts *opts, void *stream, hsmu_stats *stats);
 
 int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream);
 int hsmu_btiles_free(hsmu_btiles *t);

@@ -29,7 +29,7 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(SRC):
         tmp = SO + ".tmp%d" % os.getpid()
         cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
-               "-shared", "-o", tmp, SRC]
+               "-shared", "-o", tmp, SRC, "-lm"]
         subprocess.check_call(cmd)
         os.replace(tmp, SO)
     return SO
@@ -48,6 +48,8 @@ def lib():
         L.oracle_symbolic.argtypes = [I, P, I, P, P, P, P, P, I]
         L.oracle_numeric.restype = I
         L.oracle_numeric.argtypes = [I, P, I, P, P, P, P, P, P, P, P, P, I]
+        L.oracle_numeric_fma.restype = I
+        L.oracle_numeric_fma.argtypes = [I, P, I, P, P, P, P, P, P, P, P, P, I]
         L.oracle_abs_numeric.restype = I
         L.oracle_abs_numeric.argtypes = [I, P, I, P, P, P, P, P, P, P, P, P, I]
         L.oracle_transpose.restype = I
@@ -69,8 +71,10 @@ def products(A, B) -> int:
     return int(lib().oracle_products(A.M, _p(A.row_ptr), _p(A.col), _p(B.row_ptr)))
 
 
-def spgemm(A, B, rows: np.ndarray | None = None, nthreads: int = 0, with_abs: bool = False):
+def spgemm(A, B, rows: np.ndarray | None = None, nthreads: int = 0, with_abs: bool = False,
+           fma: bool = False):
     """C = A*B on the host (rows=None: all rows; else only the listed rows).
+    fma=True accumulates with one rounding per product (c = fma(a, b, c)).
 
     Returns (row_ptr int64[nrows+1], col int32[nnz], val float64[nnz]) and,
     with with_abs, also sum |a||b| per entry."""
@@ -91,8 +95,9 @@ def spgemm(A, B, rows: np.ndarray | None = None, nthreads: int = 0, with_abs: bo
     np.cumsum(cnt, out=rp[1:])
     col = np.empty(int(rp[-1]), dtype=np.int32)
     val = np.empty(int(rp[-1]), dtype=np.float64)
-    rc = L.oracle_numeric(nrows, _p(rows), B.N, _p(A.row_ptr), _p(A.col), _p(A.val),
-                          _p(B.row_ptr), _p(B.col), _p(B.val), _p(rp), _p(col), _p(val), nthreads)
+    num = L.oracle_numeric_fma if fma else L.oracle_numeric
+    rc = num(nrows, _p(rows), B.N, _p(A.row_ptr), _p(A.col), _p(A.val),
+             _p(B.row_ptr), _p(B.col), _p(B.val), _p(rp), _p(col), _p(val), nthreads)
     if rc:
         raise MemoryError("oracle_numeric failed: %d" % rc)
     if not with_abs:

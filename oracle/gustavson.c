@@ -31,6 +31,7 @@
  * Parallelism: OpenMP over rows, one dense sparse accumulator (SPA) per
  * thread.  The result does not depend on the thread count.
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -119,11 +120,11 @@ static int cmp_int(const void *a, const void *b)
  * Writes sorted columns to ccol and values to cval.  For each output entry
  * the value is the left-to-right sum 0.0 + p_1 + p_2 + ... where the p_t are
  * the rounded products a_ik*b_kj in the order described at the top of the
- * file. */
-int oracle_numeric(int nrows, const int *rows, int N,
-                   const int *arp, const int *acol, const double *aval,
-                   const int *brp, const int *bcol, const double *bval,
-                   const int64_t *crp, int *ccol, double *cval, int nthreads)
+ * file (fused != 0: each step is fma(a_ik, b_kj, partial sum) instead). */
+static int numeric_impl(int nrows, const int *rows, int N,
+                        const int *arp, const int *acol, const double *aval,
+                        const int *brp, const int *bcol, const double *bval,
+                        const int64_t *crp, int *ccol, double *cval, int nthreads, int fused)
 {
     int err = 0;
     set_threads(nthreads);
@@ -147,13 +148,15 @@ int oracle_numeric(int nrows, const int *rows, int N,
                     double a = aval[p];
                     for (int q = brp[k]; q < brp[k + 1]; q++) {
                         int j = bcol[q];
-                        double prod = a * bval[q]; /* rounded product */
                         if (mark[j] != r) {
                             mark[j] = r;
                             acc[j] = 0.0;
                             cols[cnt++] = j;
                         }
-                        acc[j] = acc[j] + prod; /* rounded sum, no FMA */
+                        if (fused)
+                            acc[j] = fma(a, bval[q], acc[j]); /* one rounding per product */
+                        else
+                            acc[j] = acc[j] + a * bval[q]; /* rounded product, rounded sum */
                     }
                 }
                 qsort(cols, (size_t)cnt, sizeof(int), cmp_int);
@@ -165,6 +168,27 @@ int oracle_numeric(int nrows, const int *rows, int N,
         }
     }
     return err;
+}
+
+int oracle_numeric(int nrows, const int *rows, int N,
+                   const int *arp, const int *acol, const double *aval,
+                   const int *brp, const int *bcol, const double *bval,
+                   const int64_t *crp, int *ccol, double *cval, int nthreads)
+{
+    return numeric_impl(nrows, rows, N, arp, acol, aval, brp, bcol, bval, crp, ccol, cval, nthreads, 0);
+}
+
+/* Same as oracle_numeric, with every product fused into its accumulator:
+ * c = fma(a, b, c), one rounding per product, in the same order.  This is the
+ * arithmetic of the engine's fused-multiply-add mode (opts.arith = 1); the
+ * reference rounds each product (see the top of the file), and the two differ
+ * by at most one rounding of each product. */
+int oracle_numeric_fma(int nrows, const int *rows, int N,
+                       const int *arp, const int *acol, const double *aval,
+                       const int *brp, const int *bcol, const double *bval,
+                       const int64_t *crp, int *ccol, double *cval, int nthreads)
+{
+    return numeric_impl(nrows, rows, N, arp, acol, aval, brp, bcol, bval, crp, ccol, cval, nthreads, 1);
 }
 
 /* Sum of |a_ik|*|b_kj| per output entry, in the same layout as cval; used to

@@ -90,6 +90,27 @@ def test_product_batch_matches_plain(engine):
             assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
 
 
+def test_galerkin_batch_fma_mode(engine):
+    # fused multiply-add accumulation: the oracle's fma restatement, bit for bit
+    import hsmu_gb
+
+    sides = [4, 11, 20]
+    As = [hsmu_gb.gen_poisson7(s) for s in sides]
+    PPt = [hsmu_gb.gen_aggregation(s) for s in sides]
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_GALERKIN, As, [p for p, _ in PPt], [t for _, t in PPt],
+                      arith=hsmu_gb.ARITH_FMA)
+    b.graph_launch()
+    b.status()
+    for p in range(len(sides)):
+        A, P, Pt = host(As[p]), host(PPt[p][0]), host(PPt[p][1])
+        rp, col, val = oracle.spgemm(A, P, fma=True)
+        AP = gen.CSR(A.M, P.N, rp.astype(np.int32), col, val)
+        rp, col, val = oracle.spgemm(Pt, AP, fma=True)
+        C = host(b.result(p))
+        np.testing.assert_array_equal(C.col, col)
+        assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
 def test_batch_reports_unsupported_rows(engine):
     import hsmu_gb
 

@@ -124,6 +124,21 @@ def test_learned_identical_to_plain(engine, name):
         assert st["fallback_rows"] > 0
 
 
+def test_learned_fma_mode(engine):
+    import torch
+
+    import hsmu_gb
+
+    p, margin = model_for_tests(engine)
+    A = gen.rmat(12, 16, seed=6, lo=-1.0, hi=1.0)
+    dA = hsmu_gb.DeviceCSR.from_host(A)
+    pt = torch.from_numpy(np.ascontiguousarray(p, np.float32)).cuda()
+    C = engine.spgemm_learned(dA, dA, pt, margin, arith=hsmu_gb.ARITH_FMA).to_host()
+    rp, col, val = oracle.spgemm(A, A, fma=True)
+    np.testing.assert_array_equal(C.col, col)
+    assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
 def test_learned_all_rows_fall_back(engine):
     # a model that predicts nothing fits: every non-tiny row is redone, result unchanged
     p, _ = model_for_tests(engine)

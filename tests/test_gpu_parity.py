@@ -200,3 +200,40 @@ def test_arith_modes_identical(engine, arith):
         C = run(engine, A, A, arith=arith)
         rp, col, val = oracle.spgemm(A, A)
         assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
+FMA_CASES = {
+    "lap64": lambda: (gen.laplacian2d(64, seed=0),) * 2,
+    "st27_12": lambda: (gen.stencil27(12, 3, seed=1),) * 2,
+    "rmat13": lambda: (gen.rmat(13, 16, seed=2, lo=-1.0, hi=1.0),) * 2,
+    "rmat12T": lambda: (lambda A: (A, gen.transpose(A)))(gen.rmat(12, 16, seed=3)),
+    "chunked": lambda: (gen.poisson_random(200, 30, seed=9, ncols=5000),
+                        gen.poisson_random(5000, 400, seed=10, ncols=3_000_000)),
+    "multiwindow": lambda: (gen.poisson_random(64, 200, seed=11, ncols=4000),
+                            gen.poisson_random(4000, 40, seed=12, ncols=20000)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FMA_CASES))
+def test_fma_mode(engine, name):
+    # fused multiply-add mode: bit-identical to the oracle's fma accumulation
+    # in the same order, and within the stated 1e-12 bar of the rounded-product
+    # arithmetic of the reference
+    import hsmu_gb
+
+    A, B = FMA_CASES[name]()
+    C = run(engine, A, B, arith=hsmu_gb.ARITH_FMA)
+    rp, col, val = oracle.spgemm(A, B, fma=True)
+    np.testing.assert_array_equal(C.row_ptr.astype(np.int64), rp)
+    np.testing.assert_array_equal(C.col, col)
+    assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+    ref = oracle.spgemm(A, B, with_abs=True)
+    assert_csr_equal(C, ref[:3], absv=ref[3], exact=False)
+
+
+def test_invalid_arith_rejected(engine):
+    import hsmu_gb
+
+    A = gen.laplacian2d(8, seed=0)
+    with pytest.raises(hsmu_gb.HsmuError):
+        run(engine, A, A, arith=3)
