@@ -34,8 +34,8 @@ constexpr int WIN_TCAP = 512;
 constexpr int WIN_SPAN = 4096;
 constexpr int WIN_OCCW = WIN_SPAN / 64;
 // Tiles per chunk of the CTA (large-row) kernels.
-constexpr int DCH_COUNT = 8192;   // count pass: 8 B per tile  -> 64 KB
-constexpr int DCH_STRUCT = 8192;  // structure pass: 12 B per tile -> 96 KB
+constexpr int DCH_COUNT = 4096;   // count pass: 8 B per tile  -> 32 KB (6 CTAs per SM)
+constexpr int DCH_STRUCT = 4096;  // structure pass: 12 B per tile -> 48 KB (4 CTAs per SM)
 
 // Row classes
 enum RowBin : int {

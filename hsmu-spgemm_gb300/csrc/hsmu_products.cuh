@@ -10,11 +10,11 @@
 //
 // The A entries are taken 32 at a time (one per lane); seg(p) gives the B
 // entry range [elo, ehi) that A entry p contributes to this accumulator.
-//   * long B segments (average >= 32 entries): one segment at a time, 32
-//     entries per step.  Entries of one B row have distinct columns, so a
-//     step has no slot conflicts and only a change of segment needs a warp
-//     sync.  The next step's B loads are issued before the current step's
-//     multiply/lookup/add (one-deep software pipeline).
+//   * long B segments (average >= 32 entries): one segment at a time, in
+//     chunks of up to LU steps of 32 entries.  Entries of one B row have
+//     distinct columns, so a chunk has no slot conflicts and only a change
+//     of segment needs a warp sync.  The next chunk's B loads are issued
+//     before the current chunk's multiply/lookup/add (software pipeline).
 //   * short B segments: the flat sequence of (A entry, B entry) items, 32 per
 //     step; lanes that hit the same slot in one step (__match_any_sync) add in
 //     lane order = A-entry order.
@@ -46,6 +46,9 @@ __device__ __forceinline__ double add_term(double c, double a, double t) {
     return __dadd_rn(c, t);
 }
 
+// steps of 32 B entries per chunk of the long-segment path
+constexpr int LU = 3;
+
 // SegFn:    void(int p, int k, int &elo, int &ehi)  -- called for valid lanes
 // LookupFn: int(int j) -> slot in acc, or -1 if j is not in the accumulator
 template <int AR, bool NC = true, class SegFn, class LookupFn>
@@ -69,25 +72,34 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
         if (total == 0) continue;
         unsigned todo = __ballot_sync(FULL, len > 0);
         if (total >= WARP * __popc(todo)) {
-            // ---- long segments: segment-aligned steps of 32, one-deep prefetch
+            // ---- long segments: one A entry at a time, its B entries in chunks of up
+            // to LU*32 (LU steps of 32); the next chunk's loads are issued before the
+            // current chunk is used.  Entries of one B row have distinct columns, so a
+            // chunk has no slot conflicts; a change of A entry needs a warp sync.
             int sgi = __ffs(todo) - 1;
             todo &= todo - 1;
             int es = __shfl_sync(FULL, elo, sgi), ls = __shfl_sync(FULL, len, sgi);
             double as = __shfl_sync(FULL, a, sgi);
             int off = 0;
-            int j0 = 0;
-            double b0 = 0.0;
-            if (lane < ls) {
-                j0 = ldx<NC>(bcol + es + lane);
-                b0 = ldx<NC>(bval + es + lane);
+            int jc[LU];
+            double bc[LU];
+#pragma unroll
+            for (int u = 0; u < LU; u++) {
+                const int e = u * WARP + lane;
+                jc[u] = 0;
+                bc[u] = 0.0;
+                if (e < ls) {
+                    jc[u] = ldx<NC>(bcol + es + e);
+                    bc[u] = ldx<NC>(bval + es + e);
+                }
             }
             while (true) {
-                int n_off = off + WARP, n_es = es, n_ls = ls;
+                int n_off = off + LU * WARP, n_es = es, n_ls = ls;
                 double n_as = as;
-                bool have_next = true, seg_change = false;
+                bool more = true, seg_change = false;
                 if (n_off >= ls) {
                     if (!todo) {
-                        have_next = false;
+                        more = false;
                     } else {
                         const int n_sgi = __ffs(todo) - 1;
                         todo &= todo - 1;
@@ -98,26 +110,39 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
                         seg_change = true;
                     }
                 }
-                int j1 = 0;
-                double b1 = 0.0;
-                if (have_next && n_off + lane < n_ls) {
-                    j1 = ldx<NC>(bcol + n_es + n_off + lane);
-                    b1 = ldx<NC>(bval + n_es + n_off + lane);
+                int jn[LU];
+                double bn[LU];
+#pragma unroll
+                for (int u = 0; u < LU; u++) {
+                    const int e = n_off + u * WARP + lane;
+                    jn[u] = 0;
+                    bn[u] = 0.0;
+                    if (more && e < n_ls) {
+                        jn[u] = ldx<NC>(bcol + n_es + e);
+                        bn[u] = ldx<NC>(bval + n_es + e);
+                    }
                 }
-                if (off + lane < ls) {
-                    const double pr = term<AR>(as, b0);
-                    const int q = lookup(j0);
-                    if (q >= 0) acc[q] = add_term<AR>(acc[q], as, pr);
-                    else bad = true;
+#pragma unroll
+                for (int u = 0; u < LU; u++) {
+                    if (off + u * WARP >= ls) break;  // warp-uniform: the chunk is shorter
+                    if (off + u * WARP + lane < ls) {
+                        const double pr = term<AR>(as, bc[u]);
+                        const int q = lookup(jc[u]);
+                        if (q >= 0) acc[q] = add_term<AR>(acc[q], as, pr);
+                        else bad = true;
+                    }
                 }
-                if (!have_next) break;
+                if (!more) break;
                 if (seg_change) __syncwarp();
                 es = n_es;
                 ls = n_ls;
                 as = n_as;
                 off = n_off;
-                j0 = j1;
-                b0 = b1;
+#pragma unroll
+                for (int u = 0; u < LU; u++) {
+                    jc[u] = jn[u];
+                    bc[u] = bn[u];
+                }
             }
             __syncwarp();
             continue;

@@ -36,6 +36,48 @@
 
 namespace hsmu {
 
+// Columns of output slots [p0, p1) of a tile table: msk[t] the mask of tile t
+// (0 <= t < len), base[t] its first slot -- set for empty tiles too, so base
+// is non-decreasing.  Column of bit b of tile t: cb0 + 64 t + b.  Callers give
+// each thread an equal share of the slots, so dense tiles do not serialise
+// on one thread.  Stops early (writes nothing more) on an inconsistent table.
+__device__ __forceinline__ void emit_columns(const unsigned long long *msk, const int *base, int len, int p0, int p1,
+                                             int cb0, int *__restrict__ out) {
+    if (p0 >= p1 || len <= 0) return;
+    int lo = 0, hi = len - 1;  // last tile with base <= p0: the one holding slot p0
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= p0) lo = mid;
+        else hi = mid - 1;
+    }
+    int t = lo;
+    unsigned long long m = msk[t];
+    for (int k = p0 - base[t]; k > 0 && m; k--) m &= m - 1ull;
+    for (int p = p0; p < p1; p++) {
+        while (!m) {
+            if (++t >= len) return;
+            m = msk[t];
+        }
+        out[p] = cb0 + (t << 6) + (__ffsll((long long)m) - 1);
+        m &= m - 1ull;
+    }
+}
+
+// Columns of the tiles lo..hi-1 of a tile table, one thread walking its tiles
+// (rows of the warp class: few entries per tile, the tiles split evenly).
+__device__ __forceinline__ void emit_tiles(const unsigned long long *msk, const int *base, int lo, int hi, int cb0,
+                                           int *__restrict__ out) {
+    for (int t = lo; t < hi; t++) {
+        unsigned long long m = msk[t];
+        int p = base[t];
+        const int cb = cb0 + (t << 6);
+        while (m) {
+            out[p++] = cb + (__ffsll((long long)m) - 1);
+            m &= m - 1ull;
+        }
+    }
+}
+
 // positions [b0, b1) of a bin (rows in ascending order) that hold the panel's rows lo <= i < hi
 __device__ __forceinline__ void bin_slice(const int *rows, int n, const RowOut &o, int M, int &b0, int &b1) {
     b0 = o.lo > 0 ? lower_bound_i32(rows, 0, n, o.lo) : 0;
@@ -134,26 +176,17 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
         int lastkey = -1;
         for (int t = lo; t < hi; t++) {
             const unsigned long long m = S.msk[t];
+            S.base[t] = run;
             if (m) {
-                S.base[t] = run;
                 lastkey = run / WIN_CUT;
                 run += popc64(m);
             }
         }
+        __syncwarp();
         if (nnz <= FUSE_CAP) {
             // ---- fused values: columns, then products through the same dense table
             for (int q = lane; q < nnz; q += WARP) S.acc[q] = 0.0;
-            for (int t = lo; t < hi; t++) {
-                unsigned long long m = S.msk[t];
-                if (m) {
-                    long long pos = rowbase + S.base[t];
-                    const int cb = (t0 + t) << 6;
-                    while (m) {
-                        ccol[pos++] = cb + (__ffsll((long long)m) - 1);
-                        m &= m - 1ull;
-                    }
-                }
-            }
+            emit_tiles(S.msk, S.base, lo, hi, t0 << 6, ccol + rowbase);
             __syncwarp();
             auto seg = [&](int p, int k, int &elo, int &ehi) {
                 elo = __ldg(brp + k);
@@ -215,24 +248,14 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
                 win[wbase + j] = Window{i, s0, e - s0, t0 + S.wt[j], out.mode == OUT_REDO};
             }
         }
-        for (int t = lo; t < hi; t++) {
-            unsigned long long m = S.msk[t];
-            if (m) {
-                long long pos = rowbase + S.base[t];
-                const int cb = (t0 + t) << 6;
-                while (m) {
-                    ccol[pos++] = cb + (__ffsll((long long)m) - 1);
-                    m &= m - 1ull;
-                }
-            }
-        }
+        emit_tiles(S.msk, S.base, lo, hi, t0 << 6, ccol + rowbase);
         __syncwarp();
     }
 }
 
 constexpr int SL_THREADS = 256;
 // > max windows in one chunk: DCH*64/WIN_CUT (slot cuts) + DCH/WIN_TCAP (rank cuts) + DCH/WIN_SPAN + 1
-constexpr int SL_WL = 1024;
+constexpr int SL_WL = 512;
 constexpr int SL_PER = DCH_STRUCT / SL_THREADS;
 static_assert(DCH_STRUCT % WIN_SPAN == 0, "chunks must start on window span boundaries");
 static_assert(DCH_STRUCT * 64 / WIN_CUT + DCH_STRUCT / WIN_TCAP + DCH_STRUCT / WIN_SPAN + 1 < SL_WL, "window list");
@@ -308,8 +331,8 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             long long lastkey = -1;
             for (int t = lo; t < hi; t++) {
                 const unsigned long long m = S.msk[t];
+                S.base[t] = run;
                 if (m) {
-                    S.base[t] = run;
                     lastkey = win_key(run, rank, t);
                     run += popc64(m);
                     rank++;
@@ -362,17 +385,10 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                     const int e = (j + 1 < nwin) ? S.wl[j + 1] : chunk_end;
                     win[wbase + j] = Window{i, s0, e - s0, c0 + S.wt[j], out.mode == OUT_REDO};
                 }
-                for (int t = lo; t < hi; t++) {
-                    unsigned long long m = S.msk[t];
-                    if (m) {
-                        long long p = rowbase + S.base[t];
-                        const int cb = (c0 + t) << 6;
-                        while (m) {
-                            ccol[p++] = cb + (__ffsll((long long)m) - 1);
-                            m &= m - 1ull;
-                        }
-                    }
-                }
+                const long long share = (long long)chunk_total * threadIdx.x / SL_THREADS;
+                const long long share1 = (long long)chunk_total * (threadIdx.x + 1) / SL_THREADS;
+                emit_columns(S.msk, S.base, len, run_row + (int)share, run_row + (int)share1, c0 << 6,
+                             ccol + rowbase);
             }
             run_row = chunk_end;
             tiles_row += chunk_tiles;
@@ -432,7 +448,7 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
     auto kds = arith == AR_IMUL ? k_struct_ds<AR_IMUL> : arith == AR_FMA ? k_struct_ds<AR_FMA> : k_struct_ds<AR_RN>;
     kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
         A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
-    k_struct_l<<<nsm * 2, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
+    k_struct_l<<<nsm * 4, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
                                                             win, win_cap, ctl);
 }
 

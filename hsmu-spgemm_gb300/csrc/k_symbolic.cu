@@ -135,7 +135,7 @@ void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo 
                   cudaStream_t st) {
     k_count_tiny<<<nsm * 4, TINY_THREADS, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, ri, ctl);
     k_count_ds<<<nsm * 6, DS_WARPS * 32, 0, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, ctl);
-    k_count_l<<<nsm * 3, L_THREADS, DCH_COUNT * sizeof(unsigned long long), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col,
+    k_count_l<<<nsm * 6, L_THREADS, DCH_COUNT * sizeof(unsigned long long), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col,
                                                                                    Bt.mask, ri, ctl);
 }
 

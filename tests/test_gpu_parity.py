@@ -66,7 +66,7 @@ def test_rectangular_random(engine):
 
 
 def test_chunked_wide_rows(engine):
-    # C rows spanning more than one 8192-tile chunk (N > 524288 columns)
+    # C rows spanning more than one 4096-tile chunk (N > 262144 columns)
     A = gen.poisson_random(400, 40, seed=7, ncols=2000)
     B = gen.poisson_random(2000, 60, seed=8, ncols=1_200_000)
     check(engine, A, B)
