@@ -174,6 +174,7 @@ struct PlainRun {
     int *scan_tmp = nullptr;
     Window *win = nullptr;
     long long win_cap = 0;
+    WinCursors wc{};
     int *crp = nullptr, *ccol = nullptr;
     double *cval = nullptr;
     Ctl *ctl = nullptr;
@@ -244,6 +245,18 @@ struct PlainRun {
         CKR(palloc(&ccol, (size_t)hc.nnz, st));
         CKR(palloc(&cval, (size_t)hc.nnz, st));
         CKR(palloc(&win, (size_t)win_cap, st));
+        if (hc.bin_count[BIN_L] == 0 && hc.wide_rows == 0) return HSMU_OK;  // no windows
+        return alloc_cursors(win_cap, (long long)hc.cur_bound);
+    }
+
+    int alloc_cursors(long long nwin, long long cap) {
+        if (nwin == 0) return HSMU_OK;
+        wc.cap = cap;
+        CKR(palloc(&wc.len, (size_t)nwin, st));
+        CKR(palloc(&wc.off, (size_t)nwin + 1, st));
+        CKR(palloc(&wc.total, 1, st));
+        CKR(palloc(&wc.scan_tmp, scan_tmp_ints((int)nwin), st));
+        CKR(palloc(&wc.cur, (size_t)cap, st));
         return HSMU_OK;
     }
 
@@ -255,11 +268,13 @@ struct PlainRun {
         launches += 3;
     }
 
-    // values of the windows made by the preceding structure() call
+    // values of the windows made by the preceding structure() call (none unless a row
+    // of the large class or a warp row above FUSE_CAP exists)
     void values() {
-        if (hc.nnz == 0) return;
-        launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, ctl, o.arith, h->nsm, st);
-        launches += 1;
+        if (hc.nnz == 0 || win_cap == 0 || (hc.bin_count[BIN_L] == 0 && hc.wide_rows == 0)) return;
+        launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, wc, ctl, o.arith, h->nsm,
+                       st);
+        launches += 6;  // window lengths, 3 scan, cursors, values
     }
 
     // start a new panel: its windows reuse the window buffer from slot 0
@@ -297,6 +312,11 @@ struct PlainRun {
         pfree(ri.cnnz, st);
         pfree(scan_tmp, st);
         pfree(win, st);
+        pfree(wc.len, st);
+        pfree(wc.off, st);
+        pfree(wc.total, st);
+        pfree(wc.scan_tmp, st);
+        pfree(wc.cur, st);
         pfree(crp, st);
         pfree(ccol, st);
         pfree(cval, st);
@@ -526,7 +546,8 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     unsigned char *flag = nullptr;
     double *cval = nullptr, *sval = nullptr;
     Window *win = nullptr;
-    long long win_cap = 0, spec_total = 0;
+    long long win_cap = 0, spec_total = 0, cur_cap = 0;
+    WinCursors wc{};
     Ctl hc{};
     DevCSR Ad = dev(A), Bd = dev(B);
     DevTiles Btd{};
@@ -588,6 +609,16 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     CK(palloc(&sval, (size_t)spec_total, st));
     CK(palloc(&win, (size_t)win_cap, st));
     CK(palloc(&crp, (size_t)M + 1, st));
+    // cursors of the windows of both passes (no exact count pass: every warp row above FUSE_CAP products)
+    cur_cap = 2 * (long long)(hc.cur_bound + hc.cur_bound_ds);
+    if (win_cap > 0) {
+        wc.cap = cur_cap;
+        CK(palloc(&wc.len, (size_t)win_cap, st));
+        CK(palloc(&wc.off, (size_t)win_cap + 1, st));
+        CK(palloc(&wc.total, 1, st));
+        CK(palloc(&wc.scan_tmp, scan_tmp_ints((int)win_cap), st));
+        CK(palloc(&wc.cur, (size_t)cur_cap, st));
+    }
     if (stats) cudaEventRecord(h->ev[3], st);
     // structure (+ values of warp-sized rows) into the slots; exact counts found here
     launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M}, win, win_cap, ctl,
@@ -612,7 +643,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag, 0, M}, win, win_cap, ctl,
                      o.arith, h->nsm, st);
     if (stats) cudaEventRecord(h->ev[4], st);
-    launch_numeric(Ad, Bd, crp, ccol, cval, win, win_cap, flag, scol, soff, ctl, o.arith, h->nsm, st);
+    launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, flag, scol, soff, wc, ctl, o.arith, h->nsm, st);
     CK(cudaGetLastError());
     if (stats) cudaEventRecord(h->ev[5], st);
     CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -657,8 +688,8 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
         stats->ms_total = t;
         // tiles 5, bounds + binning 6, features 1, capacity 1, scan 3, structure 3, scan 3, compact 1, redo 3,
-        // numeric 1
-        stats->launches = (o.validate ? 2 : 0) + 27;
+        // window cursors 5, numeric 1
+        stats->launches = (o.validate ? 2 : 0) + (win_cap > 0 ? 32 : 27);
     }
 done:
     pfree(ctl, st);
@@ -681,6 +712,11 @@ done:
     pfree(scol, st);
     pfree(sval, st);
     pfree(win, st);
+    pfree(wc.len, st);
+    pfree(wc.off, st);
+    pfree(wc.total, st);
+    pfree(wc.scan_tmp, st);
+    pfree(wc.cur, st);
     pfree(crp, st);
     pfree(ccol, st);
     pfree(cval, st);

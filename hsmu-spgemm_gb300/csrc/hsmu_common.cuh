@@ -77,6 +77,10 @@ struct Ctl {
     int fallback;                    // learned path: rows that did not fit their slot
     int wide_rows;                   // warp-class rows with more than FUSE_CAP entries (need windows)
     long long binned;                // rows in the bins (total of the bin scan)
+    unsigned long long cur_bound;    // bound on sum over windows of the row's A entries: large-class
+                                     // rows (bounds pass) + warp rows above FUSE_CAP (count pass)
+    unsigned long long cur_bound_ds; // same for every warp row with more than FUSE_CAP products
+                                     // (bounds pass; for paths without a count pass)
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -89,9 +89,19 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
 // flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped;
 // scol/soff (nullable): speculative slots holding the columns of speculative-pass
 // windows, which the kernel copies to ccol
-void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, int *ccol, double *cval,
+// per-window cursors into the B rows (k_win_cursors): len/off/scan_tmp sized for
+// win_cap windows (+1), cur for cap entries (Ctl::cur_bound)
+struct WinCursors {
+    int *len;
+    long long *off;
+    long long *total;
+    int *scan_tmp;
+    int *cur;
+    long long cap;
+};
+void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
-                    const long long *soff, Ctl *ctl, int arith, int nsm, cudaStream_t st);
+                    const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st);
 
 int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st);
 

@@ -14,10 +14,10 @@
 // tile's u64 column mask and first slot:
 //   slot(j) = tbase[r] + popc(tmask[r] & ((1 << (j & 63)) - 1)),
 //   r = opre[t >> 6] + popc(occ[t >> 6] & ((1 << (t & 63)) - 1)),  t = (j >> 6) - t0.
-// A warp takes GW consecutive windows; when the next window continues the
-// same row, the per-A-entry cursors into the B rows are carried over in
-// shared memory, so B rows are split at window boundaries by a short forward
-// (galloping) search instead of a fresh binary search per window.
+// Where each B row enters a window is precomputed for every (window, A entry)
+// pair by k_win_cursors, a search per pair run with all pairs in flight at
+// once; the window kernel reads its segment [cursor(w), cursor(w+1)) with two
+// loads instead of searching B rows inside its latency-bound loop.
 //
 // Accumulation order is deterministic and equals the oracle's: the products
 // of the window are walked in the flat order (A entry, then B entry), 32 per
@@ -38,8 +38,7 @@ namespace hsmu {
 
 constexpr int NUM_WARPS = 4;
 constexpr int NUM_CTAS_PER_SM = 3;
-constexpr int KCAP = 512;  // carried cursors (A entries per row)
-constexpr int GW = 8;      // consecutive windows per warp group
+constexpr int GW = 8;  // consecutive windows per warp group
 
 struct NumSmem {
     unsigned long long occ[WIN_OCCW];
@@ -47,8 +46,52 @@ struct NumSmem {
     unsigned long long tmask[WIN_TCAP];
     int tbase[WIN_TCAP];
     double acc[WIN_CAP];
-    int cur[KCAP];
 };
+
+// A entries of each window's row (0 past the emitted windows), scanned into
+// the windows' offsets in the cursor array
+__global__ void __launch_bounds__(256) k_win_len(const Window *__restrict__ win, int win_cap,
+                                                 const int *__restrict__ arp, const Ctl *ctl, int *__restrict__ len) {
+    const int nwin = min(ctl->win_count, win_cap);
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < win_cap; w += gridDim.x * blockDim.x) {
+        int n = 0;
+        if (w < nwin) {
+            const int row = win[w].row;
+            n = arp[row + 1] - arp[row];
+        }
+        len[w] = n;
+    }
+}
+
+// cursor of (window w, A entry p of its row): index of the first entry of B row
+// acol[p] whose column lies in or after the window's first tile -- found in
+// B's sorted tile list, whose tile_off gives the tile's first entry
+__global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ win, int win_cap,
+                                                     const long long *__restrict__ woff, long long cur_cap,
+                                                     const int *__restrict__ arp, const int *__restrict__ acol,
+                                                     const int *__restrict__ brp, const int *__restrict__ tptr,
+                                                     const int *__restrict__ tcol, const int *__restrict__ toff,
+                                                     int *__restrict__ wcur, Ctl *ctl) {
+    const int nwin = min(ctl->win_count, win_cap);
+    const int lane = lane_id();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = gw; w < nwin; w += nw) {
+        const Window W = win[w];
+        const int a_lo = arp[W.row], a_hi = arp[W.row + 1];
+        const long long base = woff[w];
+        if (base + (a_hi - a_lo) > cur_cap) {
+            if (lane == 0) set_err(&ctl->err, DERR_CAPACITY);
+            continue;
+        }
+        for (int p = a_lo + lane; p < a_hi; p += WARP) {
+            const int k = __ldg(acol + p);
+            const int lo = __ldg(tptr + k), hi = __ldg(tptr + k + 1);
+            const int idx = lower_bound_i32(tcol, lo, hi, W.t0);
+            wcur[base + (p - a_lo)] = idx < hi ? __ldg(toff + idx) : __ldg(brp + k + 1);
+        }
+    }
+}
 static_assert(WIN_OCCW == 2 * WARP, "prefix pass assumes two occupancy words per lane");
 
 __device__ __forceinline__ unsigned lanemask_le() { return lanemask_lt() | (1u << lane_id()); }
@@ -63,7 +106,9 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             double *__restrict__ cval, const Window *__restrict__ win,
                                                             int win_cap, const unsigned char *__restrict__ flag,
                                                             const int *__restrict__ scol,
-                                                            const long long *__restrict__ soff, Ctl *ctl) {
+                                                            const long long *__restrict__ soff,
+                                                            const long long *__restrict__ woff,
+                                                            const int *__restrict__ wcur, Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
@@ -73,20 +118,15 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
     const int nw = gridDim.x * NUM_WARPS;
     bool bad = false;
     for (int g = gw; g < ngroups; g += nw) {
-        int prev_row = -1, prev_end = -1;
         const int wend = min(nwin, (g + 1) * GW);
         for (int wi = g * GW; wi < wend; wi++) {
             const Window W = win[wi];
             const int row = W.row, cnt = W.cnt, t0 = W.t0;
-            if (flag && flag[row] == ROW_OVERFLOW && !W.redo) {  // stale: the redo pass emitted fresh windows
-                prev_row = -1;
-                continue;
-            }
+            if (flag && flag[row] == ROW_OVERFLOW && !W.redo) continue;  // stale: the redo pass emitted fresh windows
             const int row_lo = crp[row], row_hi = crp[row + 1];
             const int s0 = row_lo + W.s0;  // windows carry row-relative offsets
             if (cnt <= 0 || cnt > WIN_CAP || W.s0 < 0 || s0 + cnt > row_hi) {
                 bad = true;
-                prev_row = -1;
                 continue;
             }
             // columns of the window: in C, or (learned path, speculative pass) still in the row's
@@ -97,16 +137,18 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             const int span = (c_hi >> 6) - t0 + 1;
             if (span <= 0 || span > WIN_SPAN || (c_lo >> 6) != t0) {
                 bad = true;
-                prev_row = -1;
                 continue;
             }
             const int a_lo = arp[row], a_hi = arp[row + 1];
-            const bool first = s0 == row_lo;
             const bool last = s0 + cnt == row_hi;
-            const bool keep = (a_hi - a_lo) <= KCAP;
-            const bool carry = keep && prev_row == row && prev_end == s0;
-            prev_row = row;
-            prev_end = s0 + cnt;
+            // the next window continues this one: its cursors end this window's segments
+            bool cont = false;
+            if (!last && wi + 1 < nwin) {
+                const Window W1 = win[wi + 1];
+                cont = W1.row == row && W1.s0 == W.s0 + cnt && W1.redo == W.redo;
+            }
+            const int *__restrict__ cur0 = wcur + woff[wi];
+            const int *__restrict__ cur1 = cont ? wcur + woff[wi + 1] : nullptr;
 
             // ---- tile table from the window's sorted columns.  dense: span <= WIN_TCAP,
             // tmask/tbase indexed by tile - t0; otherwise two-level (occupancy + rank).
@@ -179,12 +221,10 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
 
             // ---- products in (A entry, B entry) order
             auto seg = [&](int p, int k, int &elo, int &ehi) {
-                const int bs = __ldg(brp + k), be = __ldg(brp + k + 1);
-                if (carry) elo = S.cur[p - a_lo];
-                else if (first) elo = bs;
-                else elo = lower_bound_i32(bcol, bs, be, c_lo);
-                ehi = last ? be : gallop_gt(bcol, elo, be, c_hi);
-                if (keep) S.cur[p - a_lo] = ehi;
+                elo = __ldg(cur0 + (p - a_lo));
+                if (cont) ehi = __ldg(cur1 + (p - a_lo));
+                else if (last) ehi = __ldg(brp + k + 1);
+                else ehi = gallop_gt(bcol, elo, __ldg(brp + k + 1), c_hi);  // next window not adjacent in the list
             };
             warp_accumulate<AR>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
             __syncwarp();
@@ -195,12 +235,18 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
     if (__any_sync(FULL, bad) && lane == 0) set_err(&ctl->err, DERR_INTERNAL);
 }
 
-void launch_numeric(const DevCSR &A, const DevCSR &B, const int *crp, int *ccol, double *cval,
+void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
-                    const long long *soff, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+                    const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+    if (win_cap <= 0) return;
+    k_win_len<<<nsm * 4, 256, 0, st>>>(win, (int)win_cap, A.rp, ctl, wc.len);
+    launch_scan64(wc.len, wc.off, (int)win_cap, wc.total, wc.scan_tmp, st);
+    k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
+                                            Bt.off, wc.cur, ctl);
     auto k = arith == AR_IMUL ? k_numeric<AR_IMUL> : arith == AR_FMA ? k_numeric<AR_FMA> : k_numeric<AR_RN>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
-        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, ctl);
+        A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, wc.off, wc.cur,
+        ctl);
 }
 
 int configure_numeric() {

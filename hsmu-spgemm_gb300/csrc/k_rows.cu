@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     __shared__ int s_cnt[NBIN];
     const int sub = threadIdx.x & (G - 1);
     const int rloc = threadIdx.x / G;
-    unsigned long long my_prod = 0, my_wb = 0;
+    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0;
     if (threadIdx.x < NBIN) s_cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int rb = blockIdx.x * RPB; rb < M; rb += gridDim.x * RPB) {
@@ -71,7 +71,11 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                 const long long cap = prod < (long long)N ? prod : (long long)N;
                 // windows per row <= slot cuts + tile-rank cuts + span cuts + 1
                 const long long tl = cap < (long long)span ? cap : (long long)span;
-                my_wb += (unsigned long long)(cap / WIN_CUT + tl / WIN_TCAP + (span - 1) / WIN_SPAN + 1);
+                const unsigned long long wb = (unsigned long long)(cap / WIN_CUT + tl / WIN_TCAP + (span - 1) / WIN_SPAN + 1);
+                my_wb += wb;
+                // rows that can reach the window pass: the large class, and warp rows above FUSE_CAP
+                if (bin == BIN_L) my_cb += wb * (unsigned long long)(arp[i + 1] - arp[i]);
+                if (bin == BIN_DS && prod > FUSE_CAP) my_cbd += wb * (unsigned long long)(arp[i + 1] - arp[i]);
             }
             ri.cls[i] = (signed char)bin;
         }
@@ -80,9 +84,13 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     if (threadIdx.x < NBIN && s_cnt[threadIdx.x]) atomicAdd(&ctl->bin_count[threadIdx.x], s_cnt[threadIdx.x]);
     my_prod = warp_sum(my_prod);
     my_wb = warp_sum(my_wb);
+    my_cb = warp_sum(my_cb);
+    my_cbd = warp_sum(my_cbd);
     if (lane_id() == 0) {
         if (my_prod) atomicAdd(&ctl->products, my_prod);
         if (my_wb) atomicAdd(&ctl->win_bound, my_wb);
+        if (my_cb) atomicAdd(&ctl->cur_bound, my_cb);
+        if (my_cbd) atomicAdd(&ctl->cur_bound_ds, my_cbd);
     }
 }
 

@@ -52,7 +52,11 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
         cnt = warp_sum(cnt);
         if (lane == 0) {
             ri.cnnz[i] = cnt;
-            if (cnt > FUSE_CAP) atomicAdd(&ctl->wide_rows, 1);
+            if (cnt > FUSE_CAP) {  // goes through numeric windows: count them for the cursor array
+                atomicAdd(&ctl->wide_rows, 1);
+                const unsigned long long wb = cnt / WIN_CUT + 1;
+                atomicAdd(&ctl->cur_bound, wb * (unsigned long long)(arp[i + 1] - arp[i]));
+            }
         }
         __syncwarp();
     }
