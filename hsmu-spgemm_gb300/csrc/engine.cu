@@ -84,8 +84,13 @@ int err_from_dev(int err) {
     if (!err) return HSMU_OK;
     if (err & DERR_UNSORTED) return HSMU_ERR_UNSORTED;
     if (err & DERR_OVERFLOW) return HSMU_ERR_OVERFLOW;
+    if (err & DERR_TIMEOUT) return HSMU_ERR_TIMEOUT;
     return HSMU_ERR_INTERNAL;
 }
+
+// C's column array: 4 ints of slack past nnz, so that the value pass can fetch a
+// window's columns in 16-byte units with bulk copies
+constexpr size_t COL_PAD = 4;
 
 bool csr_ok(const hsmu_csr *X) {
     if (!X || X->M < 0 || X->N < 0 || X->nnz < 0) return false;
@@ -242,7 +247,7 @@ struct PlainRun {
     }
 
     int alloc_output() {
-        CKR(palloc(&ccol, (size_t)hc.nnz, st));
+        CKR(palloc(&ccol, (size_t)hc.nnz + COL_PAD, st));
         CKR(palloc(&cval, (size_t)hc.nnz, st));
         CKR(palloc(&win, (size_t)win_cap, st));
         if (hc.bin_count[BIN_L] == 0 && hc.wide_rows == 0) return HSMU_OK;  // no windows
@@ -605,7 +610,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         rc = HSMU_ERR_OVERFLOW;
         goto done;
     }
-    CK(palloc(&scol, (size_t)spec_total, st));
+    CK(palloc(&scol, (size_t)spec_total + COL_PAD, st));
     CK(palloc(&sval, (size_t)spec_total, st));
     CK(palloc(&win, (size_t)win_cap, st));
     CK(palloc(&crp, (size_t)M + 1, st));
@@ -637,7 +642,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         rc = HSMU_ERR_OVERFLOW;
         goto done;
     }
-    CK(palloc(&ccol, (size_t)hc.nnz, st));
+    CK(palloc(&ccol, (size_t)hc.nnz + COL_PAD, st));
     CK(palloc(&cval, (size_t)hc.nnz, st));
     launch_compact(M, soff, crp, flag, scol, sval, ccol, cval, h->nsm, st);
     launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag, 0, M}, win, win_cap, ctl,

@@ -50,7 +50,8 @@ enum DevErr : int {
     DERR_UNSORTED = 1,
     DERR_INTERNAL = 2,
     DERR_CAPACITY = 4,
-    DERR_OVERFLOW = 8
+    DERR_OVERFLOW = 8,
+    DERR_TIMEOUT = 16  // a bounded wait (an asynchronous copy) ran out
 };
 
 struct Window {
@@ -148,6 +149,46 @@ __device__ __forceinline__ int gallop_gt(const int *__restrict__ a, int lo, int 
 }
 
 __device__ __forceinline__ void set_err(int *err, int bit) { atomicOr(err, bit); }
+
+// ---- 1-D bulk copies global -> shared memory (cp.async.bulk, the TMA unit)
+// completing on an mbarrier.  Source and destination 16-byte aligned, size a
+// multiple of 16 bytes.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// one thread: order this warp's earlier shared-memory accesses before the
+// copy's writes, arm the barrier for `bytes` and start the copy
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// wait until the barrier's phase `parity` has completed, at most `limit`
+// polls (each poll may suspend the thread for a bounded time); false if the
+// limit ran out
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int limit) {
+    for (int it = 0; it < limit; it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 // OR of a 64-bit mask into shared memory as 32-bit atomics on its halves.
 // The SM executes 32-bit shared atomics natively; the 64-bit form measured

@@ -36,17 +36,22 @@
 
 namespace hsmu {
 
-constexpr int NUM_WARPS = 4;
+constexpr int NUM_WARPS = 5;
 constexpr int NUM_CTAS_PER_SM = 3;
 constexpr int GW = 8;  // consecutive windows per warp group
+constexpr int STAGE_LIMIT = 1 << 20;  // polls of a column copy before the kernel reports a timeout
 
-struct NumSmem {
-    unsigned long long occ[WIN_OCCW];
-    int opre[WIN_OCCW];
-    unsigned long long tmask[WIN_TCAP];
-    int tbase[WIN_TCAP];
+// per warp; acc first: it also receives the window's columns by bulk copy
+// (16-byte aligned) before they are turned into the tile table
+struct alignas(16) NumSmem {
     double acc[WIN_CAP];
+    unsigned long long tmask[WIN_TCAP];
+    unsigned long long occ[WIN_OCCW];
+    unsigned long long bar;  // mbarrier of the column copy
+    int opre[WIN_OCCW];
+    unsigned short tbase[WIN_TCAP];
 };
+static_assert(WIN_CAP * 8 >= (WIN_CAP + 8) * 4, "column stage fits in the accumulator");
 
 // A entries of each window's row (0 past the emitted windows), scanned into
 // the windows' offsets in the cursor array
@@ -109,9 +114,12 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             const long long *__restrict__ soff,
                                                             const long long *__restrict__ woff,
                                                             const int *__restrict__ wcur, Ctl *ctl) {
-    extern __shared__ unsigned long long s_dyn[];
+    extern __shared__ __align__(16) unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
+    if (lane == 0) mbar_init(&S.bar);
+    __syncwarp();
+    unsigned phase = 0;
     const int nwin = min(ctl->win_count, win_cap);
     const int ngroups = (nwin + GW - 1) / GW;
     const int gw = blockIdx.x * NUM_WARPS + w;
@@ -130,9 +138,25 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 continue;
             }
             // columns of the window: in C, or (learned path, speculative pass) still in the row's
-            // slot -- then they are copied to C here while the table is built
+            // slot -- then they are copied to C here while the table is built.  One bulk copy
+            // brings them into the accumulator's space (16-byte aligned: `head` ints before)
             const bool from_slot = scol != nullptr && !W.redo;
-            const int *__restrict__ src = from_slot ? scol + soff[row] + W.s0 : ccol + s0;
+            const int *__restrict__ gsrc = from_slot ? scol + soff[row] + W.s0 : ccol + s0;
+            const uintptr_t ga = reinterpret_cast<uintptr_t>(gsrc);
+            const int lead = (int)((ga & 15u) >> 2);
+            const unsigned bytes = (unsigned)(((lead + cnt) * 4 + 15) & ~15);
+            int *stage = reinterpret_cast<int *>(S.acc);
+            __syncwarp();
+            if (lane == 0) bulk_g2s(stage, reinterpret_cast<const void *>(ga & ~(uintptr_t)15), bytes, &S.bar);
+            for (int q = lane; q < WIN_TCAP; q += WARP) S.tmask[q] = 0ull;
+            for (int q = lane; q < WIN_OCCW; q += WARP) S.occ[q] = 0ull;
+            const bool arrived = mbar_wait(&S.bar, phase, STAGE_LIMIT) || mbar_wait(&S.bar, phase, STAGE_LIMIT);
+            if (!__all_sync(FULL, arrived)) {
+                if (lane == 0) set_err(&ctl->err, DERR_TIMEOUT);
+                return;  // the copy never completed: leave the kernel
+            }
+            phase ^= 1u;
+            const int *src = stage + lead;
             const int c_lo = src[0], c_hi = src[cnt - 1];
             const int span = (c_hi >> 6) - t0 + 1;
             if (span <= 0 || span > WIN_SPAN || (c_lo >> 6) != t0) {
@@ -154,10 +178,6 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             // tmask/tbase indexed by tile - t0; otherwise two-level (occupancy + rank).
             const bool dense = span <= WIN_TCAP;
             const int nwords = (span + 63) >> 6;
-            if (!dense)
-                for (int q = lane; q < nwords; q += WARP) S.occ[q] = 0ull;
-            for (int q = lane; q < (dense ? span : min(cnt, WIN_TCAP)); q += WARP) S.tmask[q] = 0ull;
-            for (int q = lane; q < cnt; q += WARP) S.acc[q] = 0.0;
             __syncwarp();
             {
                 int run = 0, prev_t = -1;
@@ -180,7 +200,7 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                             bad = true;
                         } else {
                             if (head) {
-                                S.tbase[rank] = s;
+                                S.tbase[rank] = (unsigned short)s;
                                 if (!dense) smem_setbit64(&S.occ[t >> 6], t & 63);
                             }
                             if (first_of_run) S.tmask[rank] |= bits;
@@ -226,6 +246,9 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 else if (last) ehi = __ldg(brp + k + 1);
                 else ehi = gallop_gt(bcol, elo, __ldg(brp + k + 1), c_hi);  // next window not adjacent in the list
             };
+            // the columns are in the table now: the accumulator takes their place
+            for (int q = lane; q < cnt; q += WARP) S.acc[q] = 0.0;
+            __syncwarp();
             warp_accumulate<AR>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
             __syncwarp();
             for (int q = lane; q < cnt; q += WARP) cval[s0 + q] = S.acc[q];
