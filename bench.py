@@ -57,9 +57,9 @@ class HostCSR:
 ARITH = {"rn": 0, "fma": 1, "imul": 2}
 
 TRAFFIC = {
-    # profiles/k_struct_ds_stencil27_32_dof3.md: 447.3 MB on the 32^3 case, scaled by the
+    # profiles/k_struct_ds_stencil27_32_dof3.md: 441.5 MB on the 32^3 case, scaled by the
     # algorithmic bytes (x1.993) to the 40^3 workload
-    "stencil27_40_dof3_AA": 891.6e6,
+    "stencil27_40_dof3_AA": 879.9e6,
 }
 
 WORKLOADS = {
