@@ -58,6 +58,62 @@ __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, i
     }
 }
 
+// OR the column masks of the B tiles of the rows referenced by A entries
+// [a_lo, a_hi) into msk[t - t0] for tile ids t0 <= t < t0 + len (tiles
+// outside set `bad`); RESTRICT limits each B row to tile ids [t0, t0 + len).
+// Items are shared out as in warp_walk_tiles, OR_U steps at a time: the tile
+// ids and masks of all OR_U steps are loaded before any of them is ORed in,
+// so a warp keeps OR_U L2 round trips in flight instead of one.
+constexpr int OR_U = 4;
+
+template <bool RESTRICT>
+__device__ __forceinline__ void warp_or_tiles(int a_lo, int a_hi, int first, int stride,
+                                              const int *__restrict__ acol, const int *__restrict__ tptr,
+                                              const int *__restrict__ tcol,
+                                              const unsigned long long *__restrict__ tmask, int t0, int len,
+                                              unsigned long long *msk, bool &bad) {
+    const int lane = lane_id();
+    for (int pb = a_lo; pb < a_hi; pb += WARP) {
+        const int p = pb + lane;
+        int lo = 0, hi = 0;
+        if (p < a_hi) {
+            const int k = __ldg(acol + p);
+            lo = __ldg(tptr + k);
+            hi = __ldg(tptr + k + 1);
+            if (RESTRICT) {
+                lo = lower_bound_i32(tcol, lo, hi, t0);
+                hi = lower_bound_i32(tcol, lo, hi, t0 + len);
+            }
+        }
+        const int n = hi - lo;
+        const int incl = warp_incl_scan(n);
+        const int total = __shfl_sync(FULL, incl, WARP - 1);
+        const int excl = incl - n;
+        for (int f = first; f < total; f += stride * OR_U) {
+            int tt[OR_U];
+            unsigned long long mm[OR_U];
+#pragma unroll
+            for (int u = 0; u < OR_U; u++) {
+                const int g = f + u * stride + lane;
+                const int s = seg_of(incl, g);
+                const int idx = __shfl_sync(FULL, lo, s) + (g - __shfl_sync(FULL, excl, s));
+                tt[u] = INT_MIN;
+                mm[u] = 0ull;
+                if (g < total) {
+                    tt[u] = __ldg(tcol + idx) - t0;
+                    mm[u] = __ldg(tmask + idx);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < OR_U; u++) {
+                if (tt[u] == INT_MIN) continue;
+                if (tt[u] >= 0 && tt[u] < len) smem_or64(msk + tt[u], mm[u]);
+                else bad = true;
+            }
+        }
+    }
+}
+
 // Block-wide exclusive scans over one value per thread (blockDim.x == NT).
 // s_tmp needs NT/32 + 1 entries.  Contains __syncthreads.
 template <int NT, class T>

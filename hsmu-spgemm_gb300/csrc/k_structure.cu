@@ -133,11 +133,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
         for (int t = lane; t < span; t += WARP) S.msk[t] = 0ull;
         __syncwarp();
         bool bad = false;
-        warp_walk_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, 0, 0, [&](int idx) {
-            const int t = __ldg(tcol + idx) - t0;
-            if (t >= 0 && t < span) smem_or64(&S.msk[t], __ldg(tmask + idx));
-            else bad = true;
-        });
+        warp_or_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, tmask, t0, span, S.msk, bad);
         if (__any_sync(FULL, bad)) {
             if (lane == 0) {
                 set_err(&ctl->err, DERR_INTERNAL);
@@ -305,15 +301,10 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             for (int t = threadIdx.x; t < len; t += SL_THREADS) S.msk[t] = 0ull;
             __syncthreads();
             bool bad = false;
-            auto orfn = [&](int idx) {
-                const int t = __ldg(tcol + idx) - c0;
-                if (t >= 0 && t < len) smem_or64(&S.msk[t], __ldg(tmask + idx));
-                else bad = true;
-            };
             if (one_chunk)
-                warp_walk_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+                warp_or_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, len, S.msk, bad);
             else
-                warp_walk_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+                warp_or_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, len, S.msk, bad);
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
             const int lo = min(len, (int)threadIdx.x * SL_PER), hi = min(len, lo + SL_PER);

@@ -40,11 +40,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
         for (int t = lane; t < span; t += WARP) msk[t] = 0ull;
         __syncwarp();
         bool bad = false;
-        warp_walk_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, 0, 0, [&](int idx) {
-            const int t = __ldg(tcol + idx) - t0;
-            if (t >= 0 && t < span) smem_or64(msk + t, __ldg(tmask + idx));
-            else bad = true;
-        });
+        warp_or_tiles<false>(arp[i], arp[i + 1], 0, WARP, acol, tptr, tcol, tmask, t0, span, msk, bad);
         if (bad) set_err(&ctl->err, DERR_INTERNAL);
         __syncwarp();
         int cnt = 0;
@@ -88,15 +84,10 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
             for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) msk[t] = 0ull;
             __syncthreads();
             bool bad = false;
-            auto orfn = [&](int idx) {
-                const int t = __ldg(tcol + idx) - c0;
-                if (t >= 0 && t < c1 - c0) smem_or64(msk + t, __ldg(tmask + idx));
-                else bad = true;
-            };
             if (one_chunk)
-                warp_walk_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+                warp_or_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
             else
-                warp_walk_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, c0, c1, orfn);
+                warp_or_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
             int cnt = 0;
