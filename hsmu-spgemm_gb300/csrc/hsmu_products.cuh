@@ -48,30 +48,53 @@ __device__ __forceinline__ double add_term(double c, double a, double t) {
 
 // steps of 32 B entries per chunk of the long-segment path
 constexpr int LU = 3;
+// a group of A entries takes the long-segment path when its non-empty
+// segments average at least this many B entries (measured: the flat path
+// is as fast below it, e.g. on power-law rows)
+constexpr int LONG_SEG_MIN = 64;
 
 // SegFn:    void(int p, int k, int &elo, int &ehi)  -- called for valid lanes
 // LookupFn: int(int j) -> slot in acc, or -1 if j is not in the accumulator
-template <int AR, bool NC = true, class SegFn, class LookupFn>
+// PG: load the next group of 32 A entries before processing the current one
+// (for rows with many A entries; costs registers in the short-row kernels)
+template <int AR, bool NC = true, bool PG = false, class SegFn, class LookupFn>
 __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *__restrict__ acol,
                                                 const double *__restrict__ aval, const int *__restrict__ brp,
                                                 const int *__restrict__ bcol, const double *__restrict__ bval,
                                                 SegFn seg, LookupFn lookup, double *acc, bool &bad) {
     const int lane = lane_id();
+    // A entries 32 at a time (PG: the next group's entries and segments are
+    // loaded before the current group is processed)
+    int n_elo = 0, n_ehi = 0;
+    double n_a = 0.0;
+    if (PG && a_lo + lane < a_hi) {
+        n_a = ldx<NC>(aval + a_lo + lane);
+        seg(a_lo + lane, ldx<NC>(acol + a_lo + lane), n_elo, n_ehi);
+    }
     for (int pb = a_lo; pb < a_hi; pb += WARP) {
-        const int p = pb + lane;
         int elo = 0, ehi = 0;
         double a = 0.0;
-        if (p < a_hi) {
-            const int k = ldx<NC>(acol + p);
-            a = ldx<NC>(aval + p);
-            seg(p, k, elo, ehi);
+        if (PG) {
+            elo = n_elo;
+            ehi = n_ehi;
+            a = n_a;
+            n_elo = n_ehi = 0;
+            n_a = 0.0;
+            if (pb + WARP + lane < a_hi) {
+                const int pn = pb + WARP + lane;
+                n_a = ldx<NC>(aval + pn);
+                seg(pn, ldx<NC>(acol + pn), n_elo, n_ehi);
+            }
+        } else if (pb + lane < a_hi) {
+            a = ldx<NC>(aval + pb + lane);
+            seg(pb + lane, ldx<NC>(acol + pb + lane), elo, ehi);
         }
         const int len = ehi - elo;
         const int incl = warp_incl_scan(len);
         const int total = __shfl_sync(FULL, incl, WARP - 1);
         if (total == 0) continue;
         unsigned todo = __ballot_sync(FULL, len > 0);
-        if (total >= WARP * __popc(todo)) {
+        if (total >= LONG_SEG_MIN * __popc(todo)) {
             // ---- long segments: one A entry at a time, its B entries in chunks of up
             // to LU*32 (LU steps of 32); the next chunk's loads are issued before the
             // current chunk is used.  Entries of one B row have distinct columns, so a

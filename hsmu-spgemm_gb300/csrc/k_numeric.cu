@@ -38,7 +38,7 @@ namespace hsmu {
 
 constexpr int NUM_WARPS = 5;
 constexpr int NUM_CTAS_PER_SM = 3;
-constexpr int GW = 8;  // consecutive windows per warp group
+constexpr int GW = 4;  // consecutive windows per work item, handed out dynamically
 constexpr int STAGE_LIMIT = 1 << 20;  // polls of a column copy before the kernel reports a timeout
 
 // per warp; acc first: it also receives the window's columns by bulk copy
@@ -122,10 +122,14 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
     unsigned phase = 0;
     const int nwin = min(ctl->win_count, win_cap);
     const int ngroups = (nwin + GW - 1) / GW;
-    const int gw = blockIdx.x * NUM_WARPS + w;
-    const int nw = gridDim.x * NUM_WARPS;
     bool bad = false;
-    for (int g = gw; g < ngroups; g += nw) {
+    // window costs differ by orders of magnitude (rows with thousands of A entries):
+    // warps take the next group of windows from a counter instead of a fixed stride
+    while (true) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(&ctl->win_next, 1);
+        g = __shfl_sync(FULL, g, 0);
+        if (g >= ngroups) break;
         const int wend = min(nwin, (g + 1) * GW);
         for (int wi = g * GW; wi < wend; wi++) {
             const Window W = win[wi];
@@ -249,7 +253,7 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             // the columns are in the table now: the accumulator takes their place
             for (int q = lane; q < cnt; q += WARP) S.acc[q] = 0.0;
             __syncwarp();
-            warp_accumulate<AR>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
+            warp_accumulate<AR, true, true>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
             __syncwarp();
             for (int q = lane; q < cnt; q += WARP) cval[s0 + q] = S.acc[q];
             __syncwarp();
@@ -262,6 +266,7 @@ void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const 
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
                     const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
     if (win_cap <= 0) return;
+    cudaMemsetAsync(&ctl->win_next, 0, sizeof(int), st);
     k_win_len<<<nsm * 4, 256, 0, st>>>(win, (int)win_cap, A.rp, ctl, wc.len);
     launch_scan64(wc.len, wc.off, (int)win_cap, wc.total, wc.scan_tmp, st);
     k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
