@@ -36,30 +36,73 @@
 
 namespace hsmu {
 
-// Columns of output slots [p0, p1) of a tile table: msk[t] the mask of tile t
-// (0 <= t < len), base[t] its first slot -- set for empty tiles too, so base
-// is non-decreasing.  Column of bit b of tile t: cb0 + 64 t + b.  Callers give
-// each thread an equal share of the slots, so dense tiles do not serialise
-// on one thread.  Stops early (writes nothing more) on an inconsistent table.
-__device__ __forceinline__ void emit_columns(const unsigned long long *msk, const int *base, int len, int p0, int p1,
-                                             int cb0, int *__restrict__ out) {
-    if (p0 >= p1 || len <= 0) return;
-    int lo = 0, hi = len - 1;  // last tile with base <= p0: the one holding slot p0
+// position of the k-th set bit (k from 0) of m; m has more than k set bits
+__device__ __forceinline__ int select64(unsigned long long m, int k) {
+    const unsigned lo = (unsigned)m;
+    const int cl = __popc(lo);
+    unsigned w = lo;
+    int pos = 0;
+    if (k >= cl) {
+        w = (unsigned)(m >> 32);
+        k -= cl;
+        pos = 32;
+    }
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const int c = __popc(w & ((1u << s) - 1u));
+        if (k >= c) {
+            k -= c;
+            w >>= s;
+            pos += s;
+        }
+    }
+    return pos;
+}
+
+// Columns of output slots [s_lo, s_hi) of a tile table -- msk[t] the mask of
+// tile t (0 <= t < len), base[t] its first slot, set for empty tiles too so
+// that base is non-decreasing, column of bit b of tile t: cb0 + 64 t + b; the
+// table's slots end at `end` -- written by one warp: 32
+// consecutive slots per step, so every store instruction covers consecutive
+// addresses.  Each step looks at 32 consecutive tiles; a lane finds the tile
+// of its slot among them (last tile whose first slot is <= its slot) and the
+// column by selecting the matching set bit of the tile's mask.
+__device__ __forceinline__ void warp_emit_columns(const unsigned long long *msk, const int *base, int len, int s_lo,
+                                                  int s_hi, int end, int cb0, int *__restrict__ out) {
+    if (s_lo >= s_hi || len <= 0) return;
+    const int lane = lane_id();
+    int lo = 0, hi = len - 1;  // tile holding slot s_lo (every lane searches alike)
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (base[mid] <= p0) lo = mid;
+        if (base[mid] <= s_lo) lo = mid;
         else hi = mid - 1;
     }
-    int t = lo;
-    unsigned long long m = msk[t];
-    for (int k = p0 - base[t]; k > 0 && m; k--) m &= m - 1ull;
-    for (int p = p0; p < p1; p++) {
-        while (!m) {
-            if (++t >= len) return;
-            m = msk[t];
+    int tc = lo, pos = s_lo;
+    while (pos < s_hi) {
+        const int t = tc + lane;
+        const int b = t < len ? base[t] : end;
+        const unsigned long long m = t < len ? msk[t] : 0ull;
+        const int bend = __shfl_sync(FULL, b, WARP - 1) + popc64(__shfl_sync(FULL, m, WARP - 1));
+        if (bend <= pos) {  // these 32 tiles end before pos (a run of empty tiles): move on
+            if (tc + WARP >= len) return;  // inconsistent table: write nothing more
+            tc += WARP;
+            continue;
         }
-        out[p] = cb0 + (t << 6) + (__ffsll((long long)m) - 1);
-        m &= m - 1ull;
+        const int stop = min(min(s_hi, bend), pos + WARP);
+        const int p = pos + lane;
+        int i = 0;
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1) {
+            const int v = __shfl_sync(FULL, b, i + s);
+            if (v <= p) i += s;
+        }
+        const unsigned long long mi = __shfl_sync(FULL, m, i);
+        const int bi = __shfl_sync(FULL, b, i);
+        if (p < stop) out[p] = cb0 + ((tc + i) << 6) + select64(mi, p - bi);
+        const int last_tile = __shfl_sync(FULL, i, WARP - 1);
+        pos = stop;
+        if (pos >= bend) tc += WARP;
+        else tc += last_tile;
     }
 }
 
@@ -314,9 +357,12 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                 sum += popc64(m);
                 ntl += m != 0ull;
             }
-            int chunk_total, chunk_tiles;
-            int run = block_excl_sum<SL_THREADS>(sum, s_tmp, chunk_total) + run_row;
-            int rank = block_excl_sum<SL_THREADS>(ntl, s_tmp, chunk_tiles) + tiles_row;
+            // one scan of (slots, non-empty tiles) packed into 64 bits
+            long long packed_total;
+            const long long packed = block_excl_sum<SL_THREADS>(((long long)sum << 32) | ntl, s_ltmp, packed_total);
+            const int chunk_total = (int)(packed_total >> 32), chunk_tiles = (int)(packed_total & 0xffffffffll);
+            int run = (int)(packed >> 32) + run_row;
+            int rank = (int)(packed & 0xffffffffll) + tiles_row;
             // window key: (first slot / WIN_CUT, tile rank / WIN_TCAP, tile / WIN_SPAN),
             // packed so that it is non-decreasing along the row
             long long lastkey = -1;
@@ -376,10 +422,10 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                     const int e = (j + 1 < nwin) ? S.wl[j + 1] : chunk_end;
                     win[wbase + j] = Window{i, s0, e - s0, c0 + S.wt[j], out.mode == OUT_REDO};
                 }
-                const long long share = (long long)chunk_total * threadIdx.x / SL_THREADS;
-                const long long share1 = (long long)chunk_total * (threadIdx.x + 1) / SL_THREADS;
-                emit_columns(S.msk, S.base, len, run_row + (int)share, run_row + (int)share1, c0 << 6,
-                             ccol + rowbase);
+                const long long share = (long long)chunk_total * w / NWARP;
+                const long long share1 = (long long)chunk_total * (w + 1) / NWARP;
+                warp_emit_columns(S.msk, S.base, len, run_row + (int)share, run_row + (int)share1,
+                                  run_row + chunk_total, c0 << 6, ccol + rowbase);
             }
             run_row = chunk_end;
             tiles_row += chunk_tiles;
