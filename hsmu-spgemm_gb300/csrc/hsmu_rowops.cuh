@@ -20,6 +20,46 @@ namespace hsmu {
 
 constexpr int TINY_MAX = 32;
 
+// A entries of a tiny row handled per batch: their column ids, B row bounds
+// and first B entries are fetched in three rounds of independent loads
+// before any of them is used (a thread would otherwise wait for ~3 dependent
+// memory round trips per A entry)
+constexpr int TINY_BATCH = 8;
+
+template <bool NC, bool VALS>
+struct TinyFetch {
+    int qs[TINY_BATCH], qe[TINY_BATCH], j0[TINY_BATCH];
+    double a[TINY_BATCH], b0[TINY_BATCH];
+
+    __device__ __forceinline__ void load(int p0, int a_hi, const int *__restrict__ acol,
+                                         const double *__restrict__ aval, const int *__restrict__ brp,
+                                         const int *__restrict__ bcol, const double *__restrict__ bval) {
+        int k[TINY_BATCH];
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++) {
+            k[u] = p0 + u < a_hi ? ldx<NC>(acol + p0 + u) : -1;
+            if (VALS) a[u] = p0 + u < a_hi ? ldx<NC>(aval + p0 + u) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++) {
+            qs[u] = qe[u] = 0;
+            if (k[u] >= 0) {
+                qs[u] = ldx<NC>(brp + k[u]);
+                qe[u] = ldx<NC>(brp + k[u] + 1);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++) {
+            j0[u] = 0;
+            b0[u] = 0.0;
+            if (qs[u] < qe[u]) {
+                j0[u] = ldx<NC>(bcol + qs[u]);
+                if (VALS) b0[u] = ldx<NC>(bval + qs[u]);
+            }
+        }
+    }
+};
+
 // number of distinct columns of row (a_lo..a_hi) of A*B; -1 if the row has
 // more than TINY_MAX products (caller classified it wrongly).
 template <bool NC = true>
@@ -27,18 +67,21 @@ __device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__r
                                               const int *__restrict__ brp, const int *__restrict__ bcol, int *cols,
                                               int stride) {
     int n = 0, seen = 0;
-    for (int p = a_lo; p < a_hi; p++) {
-        const int k = ldx<NC>(acol + p);
-        const int qe = ldx<NC>(brp + k + 1);
-        for (int q = ldx<NC>(brp + k); q < qe; q++) {
-            if (++seen > TINY_MAX) return -1;
-            const int j = ldx<NC>(bcol + q);
-            int pos = n;
-            while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
-            if (pos > 0 && cols[(pos - 1) * stride] == j) continue;
-            for (int t = n; t > pos; t--) cols[t * stride] = cols[(t - 1) * stride];
-            cols[pos * stride] = j;
-            n++;
+    for (int p0 = a_lo; p0 < a_hi; p0 += TINY_BATCH) {
+        TinyFetch<NC, false> F;
+        F.load(p0, a_hi, acol, nullptr, brp, bcol, nullptr);
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++) {
+            for (int q = F.qs[u]; q < F.qe[u]; q++) {
+                if (++seen > TINY_MAX) return -1;
+                const int j = q == F.qs[u] ? F.j0[u] : ldx<NC>(bcol + q);
+                int pos = n;
+                while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
+                if (pos > 0 && cols[(pos - 1) * stride] == j) continue;
+                for (int t = n; t > pos; t--) cols[t * stride] = cols[(t - 1) * stride];
+                cols[pos * stride] = j;
+                n++;
+            }
         }
     }
     return n;
@@ -54,27 +97,31 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
                                              int *cols, double *acc, int stride, int cap, int *__restrict__ out_col,
                                              double *__restrict__ out_val) {
     int n = 0, seen = 0;
-    for (int p = a_lo; p < a_hi; p++) {
-        const int k = ldx<NC>(acol + p);
-        const double a = ldx<NC>(aval + p);
-        const int qe = ldx<NC>(brp + k + 1);
-        for (int q = ldx<NC>(brp + k); q < qe; q++) {
-            if (++seen > TINY_MAX) return -1;
-            const int j = ldx<NC>(bcol + q);
-            const double pr = term<AR>(a, ldx<NC>(bval + q));
-            int pos = n;
-            while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
-            if (pos > 0 && cols[(pos - 1) * stride] == j) {
-                acc[(pos - 1) * stride] = add_term<AR>(acc[(pos - 1) * stride], a, pr);
-                continue;
+    for (int p0 = a_lo; p0 < a_hi; p0 += TINY_BATCH) {
+        TinyFetch<NC, true> F;
+        F.load(p0, a_hi, acol, aval, brp, bcol, bval);
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++) {
+            const double a = F.a[u];
+            for (int q = F.qs[u]; q < F.qe[u]; q++) {
+                if (++seen > TINY_MAX) return -1;
+                const bool first = q == F.qs[u];
+                const int j = first ? F.j0[u] : ldx<NC>(bcol + q);
+                const double pr = term<AR>(a, first ? F.b0[u] : ldx<NC>(bval + q));
+                int pos = n;
+                while (pos > 0 && cols[(pos - 1) * stride] > j) pos--;
+                if (pos > 0 && cols[(pos - 1) * stride] == j) {
+                    acc[(pos - 1) * stride] = add_term<AR>(acc[(pos - 1) * stride], a, pr);
+                    continue;
+                }
+                for (int t = n; t > pos; t--) {
+                    cols[t * stride] = cols[(t - 1) * stride];
+                    acc[t * stride] = acc[(t - 1) * stride];
+                }
+                cols[pos * stride] = j;
+                acc[pos * stride] = add_term<AR>(0.0, a, pr);
+                n++;
             }
-            for (int t = n; t > pos; t--) {
-                cols[t * stride] = cols[(t - 1) * stride];
-                acc[t * stride] = acc[(t - 1) * stride];
-            }
-            cols[pos * stride] = j;
-            acc[pos * stride] = add_term<AR>(0.0, a, pr);
-            n++;
         }
     }
     if (n > cap) return -1;
@@ -84,7 +131,6 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
     }
     return n;
 }
-
 
 // ---------------------------------------------------------------------------
 // Warp-per-row routines on a dense span table, driven by B's entries (no B
