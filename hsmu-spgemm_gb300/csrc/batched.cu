@@ -267,14 +267,26 @@ __device__ bool phase_scan(const BParams &P, int r) {
         }
     }
     if (!grid_sync(P.bar, P.err)) return false;
-    // block scan of the chunk, in tiles of blockDim rows
+    // block scan of the chunk, in tiles of SCAN_RUN rows per thread (one block scan,
+    // three barriers, per tile of blockDim * SCAN_RUN rows)
+    constexpr int SCAN_RUN = 16;
     long long run = P.bsum[blockIdx.x];
-    for (long long b = lo; b < hi; b += blockDim.x) {
-        const long long i = b + threadIdx.x;
-        const long long x = i < hi ? R.cnnz[i] : 0;
+    for (long long b = lo; b < hi; b += (long long)blockDim.x * SCAN_RUN) {
+        const long long i0 = b + (long long)threadIdx.x * SCAN_RUN;
+        int x[SCAN_RUN];
+        long long s = 0;
+#pragma unroll
+        for (int u = 0; u < SCAN_RUN; u++) {
+            x[u] = i0 + u < hi ? R.cnnz[i0 + u] : 0;
+            s += x[u];
+        }
         long long t2;
-        const long long ex = block_excl_sum<BW * 32>(x, s_tmp, t2);
-        if (i < hi) R.excl[i] = run + ex;
+        long long e = run + block_excl_sum<BW * 32>(s, s_tmp, t2);
+#pragma unroll
+        for (int u = 0; u < SCAN_RUN; u++) {
+            if (i0 + u < hi) R.excl[i0 + u] = e;
+            e += x[u];
+        }
         run += t2;
     }
     return true;
