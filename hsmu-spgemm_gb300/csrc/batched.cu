@@ -173,11 +173,7 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
             const BOp B = b_operand(P, r, p);
             const int li = (int)(i - R.row0[p]);
             const int a_lo = ldx<NC>(A.rp + li), a_hi = ldx<NC>(A.rp + li + 1);
-            int prod = 0;
-            for (int q = a_lo; q < a_hi && prod <= P.tiny; q++) {
-                const int k = ldx<NC>(A.col + q);
-                prod += ldx<NC>(B.rp + k + 1) - ldx<NC>(B.rp + k);
-            }
+            const int prod = tiny_products<NC>(a_lo, a_hi, A.col, B.rp, P.tiny);
             if (prod > P.tiny) {
                 big = true;
             } else if (!FILL) {

@@ -60,6 +60,23 @@ struct TinyFetch {
     }
 };
 
+// intermediate products of row (a_lo..a_hi), counted until they pass `limit`,
+// TINY_BATCH A entries per round of independent loads
+template <bool NC = true>
+__device__ __forceinline__ int tiny_products(int a_lo, int a_hi, const int *__restrict__ acol,
+                                             const int *__restrict__ brp, int limit) {
+    int prod = 0;
+    for (int p0 = a_lo; p0 < a_hi && prod <= limit; p0 += TINY_BATCH) {
+        int k[TINY_BATCH];
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++) k[u] = p0 + u < a_hi ? ldx<NC>(acol + p0 + u) : -1;
+#pragma unroll
+        for (int u = 0; u < TINY_BATCH; u++)
+            if (k[u] >= 0) prod += ldx<NC>(brp + k[u] + 1) - ldx<NC>(brp + k[u]);
+    }
+    return prod;
+}
+
 // number of distinct columns of row (a_lo..a_hi) of A*B; -1 if the row has
 // more than TINY_MAX products (caller classified it wrongly).
 template <bool NC = true>
