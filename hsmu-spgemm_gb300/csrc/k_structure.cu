@@ -108,7 +108,8 @@ __device__ __forceinline__ void warp_emit_columns(const unsigned long long *msk,
 
 // Columns of the tiles lo..hi-1 of a tile table, one thread walking its tiles
 // (rows of the warp class: few entries per tile, the tiles split evenly).
-__device__ __forceinline__ void emit_tiles(const unsigned long long *msk, const int *base, int lo, int hi, int cb0,
+template <class BaseT>
+__device__ __forceinline__ void emit_tiles(const unsigned long long *msk, const BaseT *base, int lo, int hi, int cb0,
                                            int *__restrict__ out) {
     for (int t = lo; t < hi; t++) {
         unsigned long long m = msk[t];
@@ -140,16 +141,17 @@ __device__ __forceinline__ int out_limit(const RowOut &o, int i) {
 }
 
 constexpr int SDS_WARPS = 4;
-constexpr int SDS_CTAS_PER_SM = 5;
+constexpr int SDS_CTAS_PER_SM = 6;
 constexpr int SDS_WL = 64;     // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
 
 struct SdsSmem {
     unsigned long long msk[SPAN_T];
-    int base[SPAN_T];
-    int wl[SDS_WL];
-    int wt[SDS_WL];
+    unsigned short base[SPAN_T];  // slots of a warp row: at most SPAN_T * 64 = 32768
+    unsigned short wl[SDS_WL];
+    unsigned short wt[SDS_WL];
     double acc[FUSE_CAP];
 };
+static_assert(SDS_WARPS * sizeof(SdsSmem) * SDS_CTAS_PER_SM <= 227 * 1024, "CTAs per SM fit in shared memory");
 
 template <int AR>
 __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
         int lastkey = -1;
         for (int t = lo; t < hi; t++) {
             const unsigned long long m = S.msk[t];
-            S.base[t] = run;
+            S.base[t] = (unsigned short)run;
             if (m) {
                 lastkey = run / WIN_CUT;
                 run += popc64(m);
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
                     const int key = S.base[t] / WIN_CUT;
                     if (key != kk) {
                         S.wl[pos] = S.base[t];
-                        S.wt[pos] = t;
+                        S.wt[pos] = (unsigned short)t;
                         pos++;
                     }
                     kk = key;
