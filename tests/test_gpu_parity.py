@@ -102,6 +102,21 @@ def test_empty_and_degenerate(engine):
     assert C.nnz == 1 and C.val[0] == 9.0
 
 
+def test_output_beyond_int32_reported(engine):
+    # a 50,000 x 1 column times a 1 x 50,000 row: nnz(C) = 2.5e9 does not fit int32 CSR; the count
+    # pass finds it and the call fails with HSMU_ERR_OVERFLOW before allocating C (tiny inputs)
+    import hsmu_gb
+
+    n = 50_000
+    col = gen.CSR(n, 1, np.arange(n + 1, dtype=np.int32), np.zeros(n, np.int32), np.ones(n))
+    row = gen.CSR(1, n, np.array([0, n], np.int32), np.arange(n, dtype=np.int32), np.ones(n))
+    with pytest.raises(hsmu_gb.HsmuError) as e:
+        run(engine, col, row)
+    assert e.value.status == 4  # HSMU_ERR_OVERFLOW
+    # the engine stays usable afterwards
+    check(engine, gen.laplacian2d(16, seed=0), gen.laplacian2d(16, seed=0))
+
+
 def test_cancellation_kept(engine):
     # (1 1) * (1 -1)^T cancels to 0.0; the entry stays (symbolic structure)
     A = gen.CSR(1, 2, np.array([0, 2], np.int32), np.array([0, 1], np.int32), np.array([1.0, 1.0]))
