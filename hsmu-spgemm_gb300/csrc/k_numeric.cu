@@ -36,8 +36,8 @@
 
 namespace hsmu {
 
-constexpr int NUM_WARPS = 5;
-constexpr int NUM_CTAS_PER_SM = 3;
+constexpr int NUM_WARPS = 4;
+constexpr int NUM_CTAS_PER_SM = 4;
 constexpr int GW = 4;  // consecutive windows per work item, handed out dynamically
 constexpr int STAGE_LIMIT = 1 << 20;  // polls of a column copy before the kernel reports a timeout
 
