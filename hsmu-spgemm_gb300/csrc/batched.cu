@@ -173,13 +173,21 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
             const BOp B = b_operand(P, r, p);
             const int li = (int)(i - R.row0[p]);
             const int a_lo = ldx<NC>(A.rp + li), a_hi = ldx<NC>(A.rp + li + 1);
-            const int prod = tiny_products<NC>(a_lo, a_hi, A.col, B.rp, P.tiny);
+            // with the class threshold at the list capacity, the thread path is tried
+            // directly and gives up (returns -1, nothing written) on a row with more
+            // products: no separate pass over the row to classify it
+            const bool direct = P.tiny >= TINY_MAX;
+            const int prod = direct ? 0 : tiny_products<NC>(a_lo, a_hi, A.col, B.rp, P.tiny);
             if (prod > P.tiny) {
                 big = true;
             } else if (!FILL) {
                 const int c = tiny_row_count<NC>(a_lo, a_hi, A.col, B.rp, B.col, S.t.cols + lane, WARP);
-                R.cnnz[i] = c < 0 ? 0 : c;
-                if (c < 0) atomicOr(P.err, BERR_INTERNAL);
+                if (c < 0 && direct) {
+                    big = true;
+                } else {
+                    R.cnnz[i] = c < 0 ? 0 : c;
+                    if (c < 0) atomicOr(P.err, BERR_INTERNAL);
+                }
             } else {
                 const long long o = R.excl[i];
                 const int nnz = R.cnnz[i];
@@ -187,7 +195,8 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
                     const int got = tiny_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val,
                                                           S.t.cols + lane, S.t.acc + lane, WARP, nnz, R.col_pool + o,
                                                           R.val_pool + o);
-                    if (got != nnz) atomicOr(P.err, BERR_INTERNAL);
+                    if (got < 0 && direct) big = true;
+                    else if (got != nnz) atomicOr(P.err, BERR_INTERNAL);
                 }
             }
         }
