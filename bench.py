@@ -202,6 +202,22 @@ def dist_barrier(world):
         dist.barrier()
 
 
+def cpu_model():
+    """host CPU description for the baseline record (machine + model name when the kernel lists one)"""
+    import platform
+
+    name = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu model")):
+                    name = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return (platform.machine() + " " + name).strip()
+
+
 def cpu_oracle_run(A, B, max_products=1.2e9, reps=3):
     """Time the host Gustavson oracle (all host threads) on A*B or a row sample."""
     import numpy as np
@@ -226,7 +242,7 @@ def cpu_oracle_run(A, B, max_products=1.2e9, reps=3):
         oracle.spgemm(A, B, rows=rows, nthreads=nthreads)
         ts.append(time.perf_counter() - t0)
     t = statistics.median(ts)
-    return {"value": 2.0 * prods / t / 1e9, "unit": "GFLOPS", "cores": nthreads, "kind": "port",
+    return {"value": 2.0 * prods / t / 1e9, "unit": "GFLOPS", "cores": nthreads, "cpu": cpu_model(), "kind": "port",
             "sample": sample + ", median of %d" % reps, "seconds": t}
 
 
@@ -382,6 +398,23 @@ def run_engine(args):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    # the reference's own timed section excludes the conversion of B and the setup
+    conv = stage["ms_convert"] / args.steps
+    line["reference_equivalent"] = {"ms_per_step": round(ms - conv, 4),
+                                    "value": round(2.0 * products / ((ms - conv) * 1e-3) / 1e9, 3),
+                                    "note": "step time without the B tile conversion"}
+    if args.workload.endswith("_AAt"):
+        # B = A^T formed on the device (hsmu_csr_transpose); the reference transposes on the host
+        for _ in range(2):
+            eng.transpose(dA).free()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(3):
+            eng.transpose(dA, stream=stream).free()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        line["device_transpose_ms"] = round(t0.elapsed_time(t1) / 3, 4)
     print(json.dumps(line), flush=True)
 
 

@@ -910,6 +910,57 @@ int hsmu_btiles_free(hsmu_btiles *t) {
     return HSMU_OK;
 }
 
+int hsmu_csr_transpose(hsmu_handle h, const hsmu_csr *A, hsmu_csr *At, void *stream) {
+    if (!h || !csr_ok(A) || !At) return HSMU_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::memset(At, 0, sizeof(*At));
+    int rc = HSMU_OK;
+    const long long n = A->nnz;
+    int *trp = nullptr, *tcol = nullptr, *si = nullptr, *hist = nullptr, *scan_tmp = nullptr;
+    double *tval = nullptr, *sd = nullptr;
+    long long *tot = nullptr;
+    Ctl *ctl = nullptr;
+    const long long ntiles_scan = (long long)transpose_hist_ints(n) / 2;
+    CK(palloc(&trp, (size_t)A->N + 1, st));
+    CK(palloc(&tcol, (size_t)n, st));
+    CK(palloc(&tval, (size_t)n, st));
+    CK(palloc(&si, transpose_scratch_ints(n), st));
+    CK(palloc(&sd, transpose_scratch_doubles(n), st));
+    CK(palloc(&hist, transpose_hist_ints(n), st));
+    CK(palloc(&scan_tmp, scan_tmp_ints((int)ntiles_scan), st));
+    CK(palloc(&tot, 1, st));
+    CK(palloc(&ctl, 1, st));
+    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    CK((cudaError_t)launch_transpose(dev(A), trp, tcol, tval, si, sd, hist, scan_tmp, tot, ctl, h->nsm, st));
+    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h->h_ctl->err) {
+        rc = err_from_dev(h->h_ctl->err);
+        goto done;
+    }
+    At->M = A->N;
+    At->N = A->M;
+    At->nnz = A->nnz;
+    At->owned = 1;
+    At->row_ptr = trp;
+    At->col = tcol;
+    At->val = tval;
+    trp = tcol = nullptr;
+    tval = nullptr;
+done:
+    pfree(trp, st);
+    pfree(tcol, st);
+    pfree(tval, st);
+    pfree(si, st);
+    pfree(sd, st);
+    pfree(hist, st);
+    pfree(scan_tmp, st);
+    pfree(tot, st);
+    pfree(ctl, st);
+    if (rc != HSMU_OK) cudaStreamSynchronize(st);
+    return rc;
+}
+
 int hsmu_csr_free(hsmu_csr *C) {
     if (!C) return HSMU_ERR_INVALID;
     if (C->owned) {

@@ -108,4 +108,11 @@ int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned lo
 // smem sizes are set once per device (cudaFuncSetAttribute)
 int configure_kernels();
 
+// k_transpose.cu: B = A^T (rows of B in ascending column order), scratch sized by the helpers
+int launch_transpose(const DevCSR &A, int *trp, int *tcol, double *tval, int *scratch_i, double *scratch_d,
+                     int *hist, int *scan_tmp, long long *total64, Ctl *ctl, int nsm, cudaStream_t st);
+size_t transpose_scratch_ints(long long nnz);
+size_t transpose_scratch_doubles(long long nnz);
+size_t transpose_hist_ints(long long nnz);
+
 }  // namespace hsmu

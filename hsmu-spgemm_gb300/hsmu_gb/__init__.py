@@ -37,7 +37,7 @@ ARITH_RN, ARITH_FMA, ARITH_IMUL = 0, 1, 2  # hsmu_opts.arith
 
 # every symbol include/hsmu_gb.h declares (checked by the CPU test suite)
 EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_handle_destroy",
-           "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_spgemm_host", "hsmu_btiles_build", "hsmu_btiles_free",
+           "hsmu_spgemm", "hsmu_spgemm_tiled", "hsmu_spgemm_host", "hsmu_csr_transpose", "hsmu_btiles_build", "hsmu_btiles_free",
            "hsmu_csr_free", "hsmu_csr_download", "hsmu_selftest_dmul", "hsmu_btiles_build_noalloc",
            "hsmu_batch_create", "hsmu_batch_execute", "hsmu_batch_graph_launch", "hsmu_batch_status",
            "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
@@ -114,6 +114,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_spgemm_host.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr),
                                    ctypes.POINTER(c_opts), P, ctypes.POINTER(c_stats)]
     L.hsmu_btiles_build.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_btiles), P]
+    L.hsmu_csr_transpose.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), P]
     L.hsmu_btiles_free.argtypes = [ctypes.POINTER(c_btiles)]
     L.hsmu_csr_free.argtypes = [ctypes.POINTER(c_csr)]
     L.hsmu_csr_download.argtypes = [ctypes.POINTER(c_csr), P, P, P, P]
@@ -355,6 +356,13 @@ class Engine:
         self.last_stats = st.as_dict() if stats else None
         return DeviceCSR(C)
 
+
+    def transpose(self, A: DeviceCSR, stream=None) -> DeviceCSR:
+        """A^T on the device, rows in ascending column order (hsmu_csr_transpose)."""
+        C = c_csr()
+        _check(load_library().hsmu_csr_transpose(self.handle, ctypes.byref(A.desc), ctypes.byref(C),
+                                                 _stream_ptr(stream)), "hsmu_csr_transpose")
+        return DeviceCSR(C)
 
     def spgemm_host(self, A, B, out=None, *, arith: int = 0, panels: int = 0, validate: bool = False,
                     stream=None, stats: bool = False):

@@ -168,6 +168,13 @@ int hsmu_spgemm_host(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_c
                      const hsmu_opts *opts, void *stream, hsmu_stats *stats);
 
 int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream);
+
+/* At = A^T on the device, every row of At in ascending column order (a stable
+ * radix sort of A's entries by column).  At is owned by the library
+ * (hsmu_csr_free).  A must be canonical CSR.  Replaces the host transpose the
+ * reference runs before an A*A^T product: csr2csc, src/mmio_highlevel.h:194,
+ * called from src/test.cu:40-56. */
+int hsmu_csr_transpose(hsmu_handle h, const hsmu_csr *A, hsmu_csr *At, void *stream);
 int hsmu_btiles_free(hsmu_btiles *t);
 
 /* B -> 64-column bit tiles into caller-owned arrays, allocating nothing.
