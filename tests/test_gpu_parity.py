@@ -102,6 +102,14 @@ def test_empty_and_degenerate(engine):
     assert C.nnz == 1 and C.val[0] == 9.0
 
 
+@pytest.mark.parametrize("ncols", [1, 63, 1000, 4095])
+def test_narrow_outputs(engine, ncols):
+    # B->N < 4096: the reference's separate small-matrix path; here the same engine
+    A = gen.poisson_random(3000, 6, seed=ncols, ncols=2000)
+    B = gen.poisson_random(2000, min(5, ncols), seed=ncols + 1, ncols=ncols)
+    check(engine, A, B)
+
+
 def test_output_beyond_int32_reported(engine):
     # a 50,000 x 1 column times a 1 x 50,000 row: nnz(C) = 2.5e9 does not fit int32 CSR; the count
     # pass finds it and the call fails with HSMU_ERR_OVERFLOW before allocating C (tiny inputs)
