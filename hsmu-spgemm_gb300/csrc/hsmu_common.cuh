@@ -92,6 +92,8 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & (WARP - 1); }
 
+__device__ __forceinline__ unsigned lanemask_le() { return lanemask_lt() | (1u << lane_id()); }
+
 template <class T>
 __device__ __forceinline__ T warp_incl_scan(T v) {
     const int lane = lane_id();
@@ -124,6 +126,25 @@ __device__ __forceinline__ T ldx(const T *p) {
 // number of set bits of m strictly below bit b (0 <= b < 64)
 __device__ __forceinline__ int rank64(unsigned long long m, int b) {
     return __popcll(m & ((1ull << b) - 1ull));
+}
+
+// slot of column j in a tile whose column mask is m and whose first column
+// sits at slot base, or -1 when bit (j & 63) of m is clear: the shift moves
+// bit (j & 63) to bit 63, so the sign tests membership and the popcount of
+// the shifted mask counts the set bits up to and including it
+__device__ __forceinline__ int tile_slot(unsigned long long m, int base, int j) {
+    const unsigned long long sh = m << (~j & 63);
+    return (long long)sh < 0 ? base + __popcll(sh) - 1 : -1;
+}
+
+// position of the (r+1)-th lowest set bit of m (0 <= r < popc(m)): the
+// largest p with popc(m & ((1 << p) - 1)) <= r, by halving steps
+__device__ __forceinline__ int nth_set_bit(unsigned m, int r) {
+    int p = 0;
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1)
+        if (__popc(m & ((1u << (p + w)) - 1u)) <= r) p += w;
+    return p;
 }
 
 // first index in [lo, hi) with a[idx] >= key (a sorted ascending)

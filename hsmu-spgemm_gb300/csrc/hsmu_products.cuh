@@ -57,11 +57,18 @@ constexpr int LONG_SEG_MIN = 64;
 // LookupFn: int(int j) -> slot in acc, or -1 if j is not in the accumulator
 // PG: load the next group of 32 A entries before processing the current one
 // (for rows with many A entries; costs registers in the short-row kernels)
-template <int AR, bool NC = true, bool PG = false, class SegFn, class LookupFn>
+// TAG: `tag` is a byte per accumulator slot (any contents), used to find the
+// lanes of a step that share a slot; without it every multi-entry step runs
+// a full-warp match.
+// LONG: groups with long segments take the long-segment path (else every group
+// runs flat, where a step inside one segment needs no conflict test either).
+template <int AR, bool NC = true, bool PG = false, bool TAG = false, bool LONG = true, class SegFn,
+          class LookupFn>
 __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *__restrict__ acol,
                                                 const double *__restrict__ aval, const int *__restrict__ brp,
                                                 const int *__restrict__ bcol, const double *__restrict__ bval,
-                                                SegFn seg, LookupFn lookup, double *acc, bool &bad) {
+                                                SegFn seg, LookupFn lookup, double *acc, bool &bad,
+                                                unsigned char *tag = nullptr) {
     const int lane = lane_id();
     // A entries 32 at a time (PG: the next group's entries and segments are
     // loaded before the current group is processed)
@@ -93,8 +100,9 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
         const int incl = warp_incl_scan(len);
         const int total = __shfl_sync(FULL, incl, WARP - 1);
         if (total == 0) continue;
-        unsigned todo = __ballot_sync(FULL, len > 0);
-        if (total >= LONG_SEG_MIN * __popc(todo)) {
+        const unsigned ne = __ballot_sync(FULL, len > 0);
+        unsigned todo = ne;
+        if (LONG && total >= LONG_SEG_MIN * __popc(todo)) {
             // ---- long segments: one A entry at a time, its B entries in chunks of up
             // to LU*32 (LU steps of 32); the next chunk's loads are issued before the
             // current chunk is used.  Entries of one B row have distinct columns, so a
@@ -170,13 +178,32 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
             __syncwarp();
             continue;
         }
-        // ---- short segments: flat (A entry, B entry) order, 32 items per step
+        // ---- short segments: flat (A entry, B entry) order, 32 items per step.
+        // The non-empty segments are packed into lanes 0..nseg-1 (flat start
+        // st, B-entry shift d = elo - st, a).  Each step ORs the starts that
+        // fall inside it into one 32-bit mask; the segment of a lane's item is
+        // then the number of starts up to it (one popc), and a step with no
+        // start after its first item holds one A entry (no slot conflicts).
+        const int nseg = __popc(ne);
         const int excl = incl - len;
-        int sg = seg_of(incl, lane);
+        const int src = nth_set_bit(ne, min(lane, nseg - 1));
+        const int st_src = __shfl_sync(FULL, excl, src);
+        const int c_d = __shfl_sync(FULL, elo - excl, src);
+        const double c_a = __shfl_sync(FULL, a, src);
+        const int c_st = lane < nseg ? st_src : INT_MAX;
+        const unsigned le = lanemask_le();
+        auto starts = [&](int f) -> unsigned {
+            const unsigned rel = (unsigned)(c_st - f);
+            return __reduce_or_sync(FULL, rel < 32u ? 1u << rel : 0u);
+        };
+        unsigned sm = starts(0);
+        int cb = 0;  // packed segments that start before the current step
         int j = 0;
-        double b = 0.0, as = __shfl_sync(FULL, a, sg);
+        double b = 0.0, as;
         {
-            const int e = __shfl_sync(FULL, elo, sg) + (lane - __shfl_sync(FULL, excl, sg));
+            const int sg = __popc(sm & le) - 1;
+            const int e = lane + __shfl_sync(FULL, c_d, sg);
+            as = __shfl_sync(FULL, c_a, sg);
             if (lane < total) {
                 j = ldx<NC>(bcol + e);
                 b = ldx<NC>(bval + e);
@@ -184,32 +211,52 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
         }
         for (int f = 0; f < total; f += WARP) {
             const bool gv = f + lane < total;
-            int sg_n = 0, j_n = 0;
+            const bool multi = (sm >> 1) != 0u;  // a segment starts after the step's first item
+            cb += __popc(sm);
+            int j_n = 0;
             double b_n = 0.0, as_n = 0.0;
             if (f + WARP < total) {
+                sm = starts(f + WARP);
+                const int sg_n = cb + __popc(sm & le) - 1;
                 const int gn = f + WARP + lane;
-                sg_n = seg_of(incl, gn);
-                const int e = __shfl_sync(FULL, elo, sg_n) + (gn - __shfl_sync(FULL, excl, sg_n));
-                as_n = __shfl_sync(FULL, a, sg_n);
+                const int e = gn + __shfl_sync(FULL, c_d, sg_n);
+                as_n = __shfl_sync(FULL, c_a, sg_n);
                 if (gn < total) {
                     j_n = ldx<NC>(bcol + e);
                     b_n = ldx<NC>(bval + e);
                 }
             }
-            int slot = -1 - lane;
-            double pr = 0.0;
-            if (gv) {
-                pr = term<AR>(as, b);
-                const int q = lookup(j);
-                if (q >= 0) slot = q;
-                else bad = true;
-            }
-            const bool act = slot >= 0;
-            const int smin = (int)__reduce_min_sync(FULL, act ? (unsigned)sg : 64u);
-            const int smax = (int)__reduce_max_sync(FULL, act ? (unsigned)sg : 0u);
-            if (smin >= smax) {
+            // every lane multiplies and looks up (invalid lanes: b = 0, result unused)
+            const double pr = term<AR>(as, b);
+            const int q = lookup(j);
+            bad |= gv && q < 0;
+            const bool act = gv && q >= 0;
+            const int slot = act ? q : -1 - lane;
+            if (!multi) {
                 // one A entry in this step: all slots distinct
                 if (act) acc[slot] = add_term<AR>(acc[slot], as, pr);
+            } else if (TAG) {
+                // each lane stamps its id on its slot; a lane that reads back another
+                // id shares the slot with that lane.  Only such lanes are matched.
+                if (act) tag[slot] = (unsigned char)lane;
+                __syncwarp();
+                const int seen = act ? (int)tag[slot] : lane;
+                const bool lost = seen != lane;
+                const unsigned lm = __ballot_sync(FULL, lost);
+                if (lm == 0u) {
+                    if (act) acc[slot] = add_term<AR>(acc[slot], as, pr);
+                } else {
+                    const unsigned cm = lm | __reduce_or_sync(FULL, lost ? 1u << seen : 0u);
+                    const bool inc = (cm >> lane) & 1u;
+                    if (act && !inc) acc[slot] = add_term<AR>(acc[slot], as, pr);
+                    int rank = 0;
+                    if (inc) rank = __popc(__match_any_sync(cm, slot) & lanemask_lt());
+                    const int maxr = (int)__reduce_max_sync(FULL, (unsigned)rank);
+                    for (int rr = 0; rr <= maxr; rr++) {
+                        if (inc && rank == rr) acc[slot] = add_term<AR>(acc[slot], as, pr);
+                        __syncwarp();
+                    }
+                }
             } else {
                 const unsigned grp = __match_any_sync(FULL, slot);
                 const int rank = __popc(grp & lanemask_lt());
@@ -221,7 +268,6 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
                 if (act && rank == maxr) acc[slot] = add_term<AR>(acc[slot], as, pr);
             }
             __syncwarp();
-            sg = sg_n;
             j = j_n;
             b = b_n;
             as = as_n;

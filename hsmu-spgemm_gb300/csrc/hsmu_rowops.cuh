@@ -244,10 +244,7 @@ __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__r
     auto lookup = [&](int j) -> int {
         const int t = (j >> 6) - t0;
         if ((unsigned)t >= (unsigned)span) return -1;
-        const unsigned long long m = msk[t];
-        const int bit = j & 63;
-        if (!((m >> bit) & 1ull)) return -1;
-        return base[t] + rank64(m, bit);
+        return tile_slot(msk[t], base[t], j);
     };
     bool bad = false;
     warp_accumulate<AR, NC>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, acc, bad);

@@ -8,12 +8,14 @@
 //
 // Work item: a window = consecutive C tiles of one row (< WIN_CAP slots,
 // <= WIN_TCAP tiles, <= WIN_SPAN tile span), cut by the structure pass.
-// Slot lookup is O(1) through a two-level tile table rebuilt from the
-// window's sorted columns: an occupancy bitmap over the window's tile span
-// with per-word prefix counts gives a tile's rank, and the rank indexes the
-// tile's u64 column mask and first slot:
-//   slot(j) = tbase[r] + popc(tmask[r] & ((1 << (j & 63)) - 1)),
-//   r = opre[t >> 6] + popc(occ[t >> 6] & ((1 << (t & 63)) - 1)),  t = (j >> 6) - t0.
+// Slot lookup is O(1) through a tile table rebuilt from the window's sorted
+// columns.  A window spanning at most WIN_TCAP tiles (the usual case) gets a
+// dense table: the column bitmap of its span (one 32-bit shared atomic per
+// column) and each tile's first slot as a prefix count,
+//   slot(j) = tbase[t] + popc(tmask[t] & ((1 << (j & 63)) - 1)),  t = (j >> 6) - t0;
+// a wider window gets a two-level table, where an occupancy bitmap over the
+// span with per-word prefix counts gives the tile's rank r, which then
+// indexes tmask/tbase:  r = opre[t >> 6] + popc(occ[t >> 6] below bit t & 63).
 // Where each B row enters a window is precomputed for every (window, A entry)
 // pair by k_win_cursors, a search per pair run with all pairs in flight at
 // once; the window kernel reads its segment [cursor(w), cursor(w+1)) with two
@@ -21,23 +23,27 @@
 //
 // Accumulation order is deterministic and equals the oracle's: the products
 // of the window are walked in the flat order (A entry, then B entry), 32 per
-// step, one per lane; lanes that hit the same slot within a step
-// (__match_any_sync) add in lane order, which is A-entry order, so every
-// C entry is 0.0 + p_1 + p_2 + ... in the order of A(i,:) -- the same sum,
-// bit for bit, as the host Gustavson oracle.  Each product is rounded before
+// step, one per lane; lanes that hit the same slot within a step add in lane
+// order, which is A-entry order, so every C entry is 0.0 + p_1 + p_2 + ...
+// in the order of A(i,:) -- the same sum, bit for bit, as the host Gustavson
+// oracle.  A step inside one A entry's segment has distinct slots; a step
+// spanning several entries finds shared slots by stamping lane ids into a
+// byte per slot (tag) and matches only the lanes that share one.  Each product is rounded before
 // the add (no FMA contraction), as in the reference (`aval * bval` then
 // atomicAdd).  No floating-point atomics are used.
 //
-// GB300 executes FP64 at ~1.6 lane-ops/clk/SM, two orders of magnitude below
-// its int32 rate, so this kernel is bound by the FP64 pipe, not by HBM; the
-// next step's B loads are issued before the current step's lookups and adds.
+// Each product costs a B load, a table lookup and an accumulator
+// read-modify-write in shared memory: on power-law rows the kernel is bound by
+// instruction issue and shared-memory latency, not by HBM (its traffic is the
+// compulsory bytes).  The next step's B loads are issued before the current
+// step's lookups and adds.
 #include "hsmu_kernels.h"
 #include "hsmu_products.cuh"
 
 namespace hsmu {
 
-constexpr int NUM_WARPS = 4;
-constexpr int NUM_CTAS_PER_SM = 4;
+constexpr int NUM_WARPS = 3;
+constexpr int NUM_CTAS_PER_SM = 5;
 constexpr int GW = 4;  // consecutive windows per work item, handed out dynamically
 constexpr int STAGE_LIMIT = 1 << 20;  // polls of a column copy before the kernel reports a timeout
 
@@ -50,7 +56,10 @@ struct alignas(16) NumSmem {
     unsigned long long bar;  // mbarrier of the column copy
     int opre[WIN_OCCW];
     unsigned short tbase[WIN_TCAP];
+    unsigned char tag[WIN_CAP];  // slot stamps of the conflict test
 };
+// the CTAs of one SM fit its 228 KB of shared memory (1 KB reserved per CTA)
+static_assert(NUM_CTAS_PER_SM * (NUM_WARPS * sizeof(NumSmem) + 1024) <= 228 * 1024, "CTAs per SM");
 static_assert(WIN_CAP * 8 >= (WIN_CAP + 8) * 4, "column stage fits in the accumulator");
 
 // A entries of each window's row (0 past the emitted windows), scanned into
@@ -98,8 +107,6 @@ __global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ 
     }
 }
 static_assert(WIN_OCCW == 2 * WARP, "prefix pass assumes two occupancy words per lane");
-
-__device__ __forceinline__ unsigned lanemask_le() { return lanemask_lt() | (1u << lane_id()); }
 
 
 template <int AR>
@@ -183,7 +190,36 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             const bool dense = span <= WIN_TCAP;
             const int nwords = (span + 63) >> 6;
             __syncwarp();
-            {
+            if (dense) {
+                // dense: the window's column bitmap (one 32-bit shared atomic per column),
+                // then every tile's first slot as the count of columns in the tiles before it
+                for (int sb = 0; sb < cnt; sb += WARP) {
+                    const int q = sb + lane;
+                    if (q < cnt) {
+                        const int c = src[q];
+                        if (from_slot) ccol[s0 + q] = c;
+                        const int t = (c >> 6) - t0;
+                        if ((unsigned)t >= (unsigned)span) bad = true;
+                        else smem_setbit64(&S.tmask[t], c & 63);
+                    }
+                }
+                __syncwarp();
+                const int per = (span + WARP - 1) / WARP;  // tiles per lane, consecutive
+                const int q0 = lane * per, q1 = min(span, q0 + per);
+                int sum = 0;
+                for (int q = q0; q < q1; q++) sum += popc64(S.tmask[q]);
+                const int incl = warp_incl_scan(sum);
+                int run = incl - sum;
+                for (int q = q0; q < q1; q++) {
+                    S.tbase[q] = (unsigned short)run;
+                    run += popc64(S.tmask[q]);
+                }
+                if (__shfl_sync(FULL, incl, WARP - 1) != cnt) bad = true;  // repeated columns
+            } else {
+                // two-level: tiles are numbered by rank in the window.  Columns are sorted,
+                // so the lanes of one tile form a run; the run's first lane (head) stores
+                // the tile's first slot and occupancy bit, every lane sets its column's bit
+                // with a 32-bit shared atomic (a tile's bits may come from two steps)
                 int run = 0, prev_t = -1;
                 for (int sb = 0; sb < cnt; sb += WARP) {
                     const int s = sb + lane;
@@ -192,27 +228,22 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                     if (v && from_slot) ccol[s0 + s] = c;
                     const int t = (c >> 6) - t0;
                     const int t_up = __shfl_up_sync(FULL, t, 1);
-                    const int tp = lane == 0 ? prev_t : t_up;
-                    const bool head = v && t != tp;
+                    const bool head = v && t != (lane == 0 ? prev_t : t_up);
                     const unsigned heads = __ballot_sync(FULL, head);
-                    const int rank = dense ? t : run + __popc(heads & lanemask_le()) - 1;
-                    // columns are sorted: lanes of one tile are a run; its first lane stores the OR
-                    const unsigned long long bits = warp_run_or(v ? t : INT_MAX, v ? 1ull << (c & 63) : 0ull);
-                    const bool first_of_run = v && (lane == 0 || t != t_up);
+                    const int rank = run + __popc(heads & lanemask_le()) - 1;
+                    run += __popc(heads);
                     if (v) {
-                        if (t < 0 || t >= span || rank < 0 || rank >= WIN_TCAP) {
+                        if ((unsigned)t >= (unsigned)span || (unsigned)rank >= (unsigned)WIN_TCAP) {
                             bad = true;
                         } else {
                             if (head) {
                                 S.tbase[rank] = (unsigned short)s;
-                                if (!dense) smem_setbit64(&S.occ[t >> 6], t & 63);
+                                smem_setbit64(&S.occ[t >> 6], t & 63);
                             }
-                            if (first_of_run) S.tmask[rank] |= bits;
+                            smem_setbit64(&S.tmask[rank], c & 63);
                         }
                     }
-                    run += __popc(heads);
                     prev_t = __shfl_sync(FULL, t, min(WARP, cnt - sb) - 1);
-                    __syncwarp();
                 }
             }
             __syncwarp();
@@ -228,19 +259,17 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             }
             __syncwarp();
             // slot of column j, or -1 when j is not in the window (corrupt input)
+            // two-level table (span > WIN_TCAP): occupancy bit and rank of the tile, then its
+            // mask; branch-free, an absent tile or column gives -1
             auto lookup = [&](int j) -> int {
-                const int t = (j >> 6) - t0;
-                if ((unsigned)t >= (unsigned)span) return -1;
-                int r = t;
-                if (!dense) {
-                    const unsigned long long ow = S.occ[t >> 6];
-                    if (!((ow >> (t & 63)) & 1ull)) return -1;
-                    r = S.opre[t >> 6] + rank64(ow, t & 63);
-                }
-                const unsigned long long m = S.tmask[r];
-                const int bit = j & 63;
-                if (!((m >> bit) & 1ull)) return -1;
-                return S.tbase[r] + rank64(m, bit);
+                const unsigned t = (unsigned)((j >> 6) - t0);
+                const bool in = t < (unsigned)span;
+                const int tc = in ? (int)t : 0;
+                const unsigned long long sh = S.occ[tc >> 6] << (~tc & 63);
+                const bool has = in && (long long)sh < 0;
+                const int r = has ? S.opre[tc >> 6] + __popcll(sh) - 1 : 0;
+                const int q = tile_slot(S.tmask[r], S.tbase[r], j);
+                return has ? q : -1;
             };
 
             // ---- products in (A entry, B entry) order
@@ -253,7 +282,21 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             // the columns are in the table now: the accumulator takes their place
             for (int q = lane; q < cnt; q += WARP) S.acc[q] = 0.0;
             __syncwarp();
-            warp_accumulate<AR, true, true>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc, bad);
+            if (dense) {
+                // branch-free: an out-of-span column reads tile 0 and is rejected
+                auto lookup_d = [&](int j) -> int {
+                    const unsigned t = (unsigned)((j >> 6) - t0);
+                    const bool in = t < (unsigned)span;
+                    const int tc = in ? (int)t : 0;
+                    const int q = tile_slot(S.tmask[tc], S.tbase[tc], j);
+                    return in ? q : -1;
+                };
+                warp_accumulate<AR, true, true, true, false>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup_d, S.acc,
+                                                      bad, S.tag);
+            } else {
+                warp_accumulate<AR, true, true, true, false>(a_lo, a_hi, acol, aval, brp, bcol, bval, seg, lookup, S.acc,
+                                                      bad, S.tag);
+            }
             __syncwarp();
             for (int q = lane; q < cnt; q += WARP) cval[s0 + q] = S.acc[q];
             __syncwarp();

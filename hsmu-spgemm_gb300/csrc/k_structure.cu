@@ -236,10 +236,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             auto lookup = [&](int j) -> int {
                 const int t = (j >> 6) - t0;
                 if ((unsigned)t >= (unsigned)span) return -1;
-                const unsigned long long m = S.msk[t];
-                const int bit = j & 63;
-                if (!((m >> bit) & 1ull)) return -1;
-                return S.base[t] + rank64(m, bit);
+                return tile_slot(S.msk[t], S.base[t], j);
             };
             bool vbad = false;
             warp_accumulate<AR>(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, seg, lookup, S.acc, vbad);
