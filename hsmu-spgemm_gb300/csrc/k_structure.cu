@@ -36,73 +36,25 @@
 
 namespace hsmu {
 
-// position of the k-th set bit (k from 0) of m; m has more than k set bits
-__device__ __forceinline__ int select64(unsigned long long m, int k) {
-    const unsigned lo = (unsigned)m;
-    const int cl = __popc(lo);
-    unsigned w = lo;
-    int pos = 0;
-    if (k >= cl) {
-        w = (unsigned)(m >> 32);
-        k -= cl;
-        pos = 32;
-    }
-#pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) {
-        const int c = __popc(w & ((1u << s) - 1u));
-        if (k >= c) {
-            k -= c;
-            w >>= s;
-            pos += s;
-        }
-    }
-    return pos;
-}
-
-// Columns of output slots [s_lo, s_hi) of a tile table -- msk[t] the mask of
-// tile t (0 <= t < len), base[t] its first slot, set for empty tiles too so
-// that base is non-decreasing, column of bit b of tile t: cb0 + 64 t + b; the
-// table's slots end at `end` -- written by one warp: 32
-// consecutive slots per step, so every store instruction covers consecutive
-// addresses.  Each step looks at 32 consecutive tiles; a lane finds the tile
-// of its slot among them (last tile whose first slot is <= its slot) and the
-// column by selecting the matching set bit of the tile's mask.
-__device__ __forceinline__ void warp_emit_columns(const unsigned long long *msk, const int *base, int len, int s_lo,
-                                                  int s_hi, int end, int cb0, int *__restrict__ out) {
-    if (s_lo >= s_hi || len <= 0) return;
+// Columns of a tile table (msk[t], first slot base[t], 0 <= t < len) written
+// by the warps of a block: 32-tile groups go round-robin to the warps, a lane
+// takes one tile of its group and writes the tile's columns lowest bit first;
+// a group takes as many steps as its fullest tile has columns.
+__device__ __forceinline__ void block_emit_tiles(const unsigned long long *msk, const int *base, int len, int warp,
+                                                 int nwarps, int cb0, int *__restrict__ out) {
     const int lane = lane_id();
-    int lo = 0, hi = len - 1;  // tile holding slot s_lo (every lane searches alike)
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (base[mid] <= s_lo) lo = mid;
-        else hi = mid - 1;
-    }
-    int tc = lo, pos = s_lo;
-    while (pos < s_hi) {
-        const int t = tc + lane;
-        const int b = t < len ? base[t] : end;
-        const unsigned long long m = t < len ? msk[t] : 0ull;
-        const int bend = __shfl_sync(FULL, b, WARP - 1) + popc64(__shfl_sync(FULL, m, WARP - 1));
-        if (bend <= pos) {  // these 32 tiles end before pos (a run of empty tiles): move on
-            if (tc + WARP >= len) return;  // inconsistent table: write nothing more
-            tc += WARP;
-            continue;
+    for (int tb = warp * WARP; tb < len; tb += nwarps * WARP) {
+        const int t = tb + lane;
+        unsigned long long m = t < len ? msk[t] : 0ull;
+        int *o = out + (t < len ? base[t] : 0);
+        const int cb = cb0 + (t << 6);
+        const int n = (int)__reduce_max_sync(FULL, (unsigned)popc64(m));
+        for (int k = 0; k < n; k++) {
+            if (m) {
+                *o++ = cb + (__ffsll((long long)m) - 1);
+                m &= m - 1ull;
+            }
         }
-        const int stop = min(min(s_hi, bend), pos + WARP);
-        const int p = pos + lane;
-        int i = 0;
-#pragma unroll
-        for (int s = 16; s >= 1; s >>= 1) {
-            const int v = __shfl_sync(FULL, b, i + s);
-            if (v <= p) i += s;
-        }
-        const unsigned long long mi = __shfl_sync(FULL, m, i);
-        const int bi = __shfl_sync(FULL, b, i);
-        if (p < stop) out[p] = cb0 + ((tc + i) << 6) + select64(mi, p - bi);
-        const int last_tile = __shfl_sync(FULL, i, WARP - 1);
-        pos = stop;
-        if (pos >= bend) tc += WARP;
-        else tc += last_tile;
     }
 }
 
@@ -421,10 +373,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                     const int e = (j + 1 < nwin) ? S.wl[j + 1] : chunk_end;
                     win[wbase + j] = Window{i, s0, e - s0, c0 + S.wt[j], out.mode == OUT_REDO};
                 }
-                const long long share = (long long)chunk_total * w / NWARP;
-                const long long share1 = (long long)chunk_total * (w + 1) / NWARP;
-                warp_emit_columns(S.msk, S.base, len, run_row + (int)share, run_row + (int)share1,
-                                  run_row + chunk_total, c0 << 6, ccol + rowbase);
+                block_emit_tiles(S.msk, S.base, len, w, NWARP, c0 << 6, ccol + rowbase);
             }
             run_row = chunk_end;
             tiles_row += chunk_tiles;
