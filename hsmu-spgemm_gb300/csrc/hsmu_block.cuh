@@ -135,6 +135,42 @@ __device__ __forceinline__ T block_excl_sum(T v, T *s_tmp, T &total) {
     return r;
 }
 
+// One-barrier variants: the warp totals go to s_w (NT/32 entries) and every
+// thread adds up the ones before its warp itself.  s_w must not be written
+// again before the next block-wide barrier (use a separate array per scan).
+template <int NT, class T>
+__device__ __forceinline__ T block_excl_sum1(T v, T *s_w, T &total) {
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    const T incl = warp_incl_scan(v);
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    T off = T(0), tot = T(0);
+#pragma unroll
+    for (int j = 0; j < NT / 32; j++) {
+        const T x = s_w[j];
+        if (j < w) off += x;
+        tot += x;
+    }
+    total = tot;
+    return off + incl - v;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_incl_max(T v);
+
+// exclusive max-scan with one barrier; threads before the first contribute `ident`
+template <int NT, class T>
+__device__ __forceinline__ T block_excl_max1(T v, T *s_w, T ident) {
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+    const T incl = warp_incl_max(v);
+    T ex = __shfl_up_sync(FULL, incl, 1);
+    if (lane == 0) ex = ident;
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    for (int j = 0; j < w; j++) ex = max(ex, s_w[j]);
+    return ex;
+}
+
 template <class T>
 __device__ __forceinline__ T warp_incl_max(T v) {
     const int lane = lane_id();

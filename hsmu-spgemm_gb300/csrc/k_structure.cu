@@ -271,8 +271,9 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                                                          Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     SlSmem &S = *reinterpret_cast<SlSmem *>(s_dyn);
-    __shared__ int s_tmp[SL_THREADS / 32 + 1];
-    __shared__ long long s_ltmp[SL_THREADS / 32 + 1];
+    // warp totals of the three block scans of a chunk (one array each: one barrier per scan)
+    __shared__ long long s_w0[SL_THREADS / 32], s_w1[SL_THREADS / 32];
+    __shared__ int s_w2[SL_THREADS / 32];
     __shared__ int s_wbase;
     constexpr int NWARP = SL_THREADS / 32;
     const int w = threadIdx.x >> 5;
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             }
             // one scan of (slots, non-empty tiles) packed into 64 bits
             long long packed_total;
-            const long long packed = block_excl_sum<SL_THREADS>(((long long)sum << 32) | ntl, s_ltmp, packed_total);
+            const long long packed = block_excl_sum1<SL_THREADS>(((long long)sum << 32) | ntl, s_w0, packed_total);
             const int chunk_total = (int)(packed_total >> 32), chunk_tiles = (int)(packed_total & 0xffffffffll);
             int run = (int)(packed >> 32) + run_row;
             int rank = (int)(packed & 0xffffffffll) + tiles_row;
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                     rank++;
                 }
             }
-            const long long carry = block_excl_max<SL_THREADS>(lastkey, s_ltmp, -1ll);
+            const long long carry = block_excl_max1<SL_THREADS>(lastkey, s_w1, -1ll);
             int nst = 0;
             {
                 long long kk = carry;
@@ -339,7 +340,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
                     }
             }
             int nwin;
-            int pos = block_excl_sum<SL_THREADS>(nst, s_tmp, nwin);
+            int pos = block_excl_sum1<SL_THREADS>(nst, s_w2, nwin);
             {
                 long long kk = carry;
                 int rk = rank - ntl;
