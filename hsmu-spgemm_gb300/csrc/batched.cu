@@ -47,9 +47,10 @@ constexpr int B_FUSE_CAP = 512;  // nnz of a warp-path row in a batch
 constexpr unsigned long long SPIN_LIMIT = 1ull << 25;
 enum BatchErr : int { BERR_TIMEOUT = 16, BERR_UNSUPPORTED = 32, BERR_CAPACITY = 64, BERR_INTERNAL = 128 };
 
-struct BOp {  // one CSR operand on the device
+struct BOp {  // one CSR operand on the device; row k is rp[k] .. re[k]-1 (re = rp + 1 for CSR)
     int M, N;
     const int *rp;
+    const int *re;
     const int *col;
     const double *val;
 };
@@ -68,6 +69,12 @@ struct BRound {
     int *col_pool;         // [cap]
     double *val_pool;      // [cap]
     long long cap;
+    // padded round (the A*P of Galerkin products, read only by the next round): every
+    // row has a slot of its product bound, excl holds the slots' offsets (set once at
+    // creation), rp_pool their starts within the product; one fill pass writes the row,
+    // its count (cnnz) and its end (re_pool).  No count pass, no scan.
+    int padded;
+    int *re_pool;          // [rpo[nprod]] (padded rounds)
 };
 
 struct GridBar {
@@ -138,6 +145,7 @@ __device__ __forceinline__ BOp b_operand(const BParams &P, int r, int p) {
     b.M = (int)(Q.row0[p + 1] - r0);
     b.N = -1;  // not needed by the row routines
     b.rp = Q.rp_pool + Q.rpo[p];
+    b.re = Q.padded ? Q.re_pool + Q.rpo[p] : b.rp + 1;
     b.col = Q.col_pool + base;
     b.val = Q.val_pool + base;
     return b;
@@ -159,8 +167,14 @@ struct BWarpSmem {
     };
 };
 
-template <int AR, bool FILL, bool NC>
+enum RowMode { RM_COUNT = 0, RM_FILL = 1, RM_PADDED = 2 };
+
+// one pass over the rows of round r: COUNT (exact nnz), FILL (columns and
+// values at the scanned offsets) or PADDED (fill at the row's bound slot,
+// recording its nnz and end)
+template <int AR, int MODE, bool NC>
 __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
+    constexpr bool FILL = MODE != RM_COUNT;
     const BRound &R = P.rnd[r];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     const long long step = (long long)gridDim.x * BW * WARP;
@@ -177,22 +191,35 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
             // directly and gives up (returns -1, nothing written) on a row with more
             // products: no separate pass over the row to classify it
             const bool direct = P.tiny >= TINY_MAX;
-            const int prod = direct ? 0 : tiny_products<NC>(a_lo, a_hi, A.col, B.rp, P.tiny);
+            const int prod = direct ? 0 : tiny_products<NC>(a_lo, a_hi, A.col, B.rp, B.re, P.tiny);
             if (prod > P.tiny) {
                 big = true;
             } else if (!FILL) {
-                const int c = tiny_row_count<NC>(a_lo, a_hi, A.col, B.rp, B.col, S.t.cols + lane, WARP);
+                const int c = tiny_row_count<NC>(a_lo, a_hi, A.col, B.rp, B.re, B.col, S.t.cols + lane, WARP);
                 if (c < 0 && direct) {
                     big = true;
                 } else {
                     R.cnnz[i] = c < 0 ? 0 : c;
                     if (c < 0) atomicOr(P.err, BERR_INTERNAL);
                 }
+            } else if (MODE == RM_PADDED) {
+                const long long o = R.excl[i];
+                const int cap = (int)(R.excl[i + 1] - o);
+                const int got = tiny_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.re, B.col, B.val,
+                                                      S.t.cols + lane, S.t.acc + lane, WARP, cap, R.col_pool + o,
+                                                      R.val_pool + o);
+                if (got < 0) {
+                    big = true;  // more than TINY_MAX products (a slot always holds the row)
+                } else {
+                    const long long at = R.rpo[p] + li;
+                    R.cnnz[i] = got;
+                    R.re_pool[at] = R.rp_pool[at] + got;
+                }
             } else {
                 const long long o = R.excl[i];
                 const int nnz = R.cnnz[i];
                 if (o + nnz <= R.cap) {
-                    const int got = tiny_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val,
+                    const int got = tiny_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.re, B.col, B.val,
                                                           S.t.cols + lane, S.t.acc + lane, WARP, nnz, R.col_pool + o,
                                                           R.val_pool + o);
                     if (got < 0 && direct) big = true;
@@ -212,7 +239,7 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
             const int li = (int)(ib - R.row0[p]);
             const int a_lo = ldx<NC>(A.rp + li), a_hi = ldx<NC>(A.rp + li + 1);
             int cmin, cmax, prod;
-            warp_row_extent<NC>(a_lo, a_hi, A.col, B.rp, B.col, cmin, cmax, prod);
+            warp_row_extent<NC>(a_lo, a_hi, A.col, B.rp, B.re, B.col, cmin, cmax, prod);
             const int t0 = cmin >> 6;
             const int span = (cmax >> 6) - t0 + 1;
             if (span > SPAN_T) {
@@ -220,7 +247,7 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
                 if (!FILL && lane == 0) R.cnnz[ib] = 0;
                 continue;
             }
-            if (!warp_row_masks<NC>(a_lo, a_hi, A.col, B.rp, B.col, t0, span, S.w.msk)) {
+            if (!warp_row_masks<NC>(a_lo, a_hi, A.col, B.rp, B.re, B.col, t0, span, S.w.msk)) {
                 if (lane == 0) atomicOr(P.err, BERR_INTERNAL);
                 continue;
             }
@@ -230,10 +257,24 @@ __device__ void phase_rows(const BParams &P, int r, BWarpSmem &S) {
                 if (c > B_FUSE_CAP && lane == 0) atomicOr(P.err, BERR_UNSUPPORTED);
             } else {
                 const long long o = R.excl[ib];
-                const int nnz = R.cnnz[ib];
+                int nnz;
+                if (MODE == RM_PADDED) {
+                    nnz = warp_mask_count(S.w.msk, span);
+                    if (nnz > B_FUSE_CAP || o + nnz > R.excl[ib + 1]) {
+                        if (lane == 0) atomicOr(P.err, nnz > B_FUSE_CAP ? BERR_UNSUPPORTED : BERR_INTERNAL);
+                        continue;
+                    }
+                    if (lane == 0) {
+                        const long long at = R.rpo[p] + li;
+                        R.cnnz[ib] = nnz;
+                        R.re_pool[at] = R.rp_pool[at] + nnz;
+                    }
+                } else {
+                    nnz = R.cnnz[ib];
+                }
                 if (nnz <= B_FUSE_CAP && o + nnz <= R.cap) {
-                    if (!warp_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.col, B.val, t0, span, S.w.msk,
-                                                S.w.base, S.w.acc, nnz, R.col_pool + o, R.val_pool + o) &&
+                    if (!warp_row_fill<AR, NC>(a_lo, a_hi, A.col, A.val, B.rp, B.re, B.col, B.val, t0, span,
+                                                S.w.msk, S.w.base, S.w.acc, nnz, R.col_pool + o, R.val_pool + o) &&
                         lane == 0)
                         atomicOr(P.err, BERR_INTERNAL);
                 }
@@ -318,15 +359,19 @@ __global__ void __launch_bounds__(BW * 32) k_batch(BParams P) {
     BWarpSmem &S = reinterpret_cast<BWarpSmem *>(s_dyn)[threadIdx.x >> 5];
     for (int r = 0; r < P.nrounds; r++) {
         if (r > 0 && !grid_sync(P.bar, P.err)) return;
-        if (r == 0) phase_rows<AR, false, true>(P, r, S);
-        else phase_rows<AR, false, false>(P, r, S);
+        if (P.rnd[r].padded) {  // only round 0 (operands from the caller) is ever padded
+            phase_rows<AR, RM_PADDED, true>(P, r, S);
+            continue;
+        }
+        if (r == 0) phase_rows<AR, RM_COUNT, true>(P, r, S);
+        else phase_rows<AR, RM_COUNT, false>(P, r, S);
         if (!grid_sync(P.bar, P.err)) return;
         if (!phase_scan(P, r)) return;
         if (!grid_sync(P.bar, P.err)) return;
         if (*(volatile int *)P.err & BERR_CAPACITY) return;
         phase_rowptr(P, r);
-        if (r == 0) phase_rows<AR, true, true>(P, r, S);
-        else phase_rows<AR, true, false>(P, r, S);
+        if (r == 0) phase_rows<AR, RM_FILL, true>(P, r, S);
+        else phase_rows<AR, RM_FILL, false>(P, r, S);
     }
 }
 
@@ -352,6 +397,20 @@ __global__ void k_batch_bound(const BOp *A, const BOp *B, const long long *row0,
     }
     my = warp_sum(my);
     if (lane_id() == 0 && my) atomicAdd(total, my);
+}
+
+// starts of the padded rows of a round within their product (from the scanned bounds)
+__global__ void k_pad_starts(const long long *row0, int nprod, long long R, const long long *excl,
+                             const long long *rpo, int *rp) {
+    const long long nthr = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < R; i += nthr) {
+        const int p = find_prod(row0, nprod, i);
+        const long long r0 = row0[p];
+        rp[rpo[p] + (i - r0)] = (int)(excl[i] - excl[r0]);
+        if (i == row0[p + 1] - 1) rp[rpo[p] + (i - r0) + 1] = (int)(excl[i + 1] - excl[r0]);
+    }
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nprod; p += (int)nthr)
+        if (row0[p + 1] == row0[p]) rp[rpo[p]] = 0;
 }
 
 __global__ void k_batch_bound2(const BOp *Pt, const long long *row0_2, const long long *row0_1, int nprod, long long R,
@@ -480,8 +539,8 @@ int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const h
             b->ncol[r][p] = B[p].N;
         }
         for (int p = 0; p < n; p++) {
-            hA[p] = BOp{L[p].M, L[p].N, L[p].row_ptr, L[p].col, L[p].val};
-            hB[p] = BOp{B[p].M, B[p].N, B[p].row_ptr, B[p].col, B[p].val};
+            hA[p] = BOp{L[p].M, L[p].N, L[p].row_ptr, L[p].row_ptr + 1, L[p].col, L[p].val};
+            hB[p] = BOp{B[p].M, B[p].N, B[p].row_ptr, B[p].row_ptr + 1, B[p].col, B[p].val};
         }
         if (balloc(b, &dA, n) || balloc(b, &dB, n) || balloc(b, &drow0[r], n + 1) || balloc(b, &drpo[r], n + 1)) {
             rc = HSMU_ERR_ALLOC;
@@ -541,6 +600,29 @@ int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const h
     if (balloc(b, &b->P.bsum, (size_t)b->grid + 1) || balloc(b, &b->P.bar, 1) || balloc(b, &b->P.err, 1)) {
         rc = HSMU_ERR_ALLOC;
         goto fail;
+    }
+    // Galerkin: A*P is read only by the second round, so its rows go straight into slots of
+    // their product bound (offsets = scan of the bounds, fixed for the batch's lifetime)
+    if (nr == 2 && b->P.rnd[0].R <= INT_MAX && htot[0] <= (unsigned long long)INT_MAX) {
+        BRound &R0 = b->P.rnd[0];
+        int *scan_tmp = nullptr;
+        long long *tot64 = nullptr;
+        if (balloc(b, &R0.re_pool, (size_t)b->rpo[0][n]) || balloc(b, &scan_tmp, scan_tmp_ints((int)R0.R)) ||
+            balloc(b, &tot64, 1)) {
+            rc = HSMU_ERR_ALLOC;
+            goto fail;
+        }
+        launch_scan64(rowbound, R0.excl, (int)R0.R, tot64, scan_tmp, st);
+        k_pad_starts<<<b->nsm * 8, 256, 0, st>>>(R0.row0, n, R0.R, R0.excl, R0.rpo, R0.rp_pool);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+            rc = HSMU_ERR_CUDA;
+            goto fail;
+        }
+        for (void *q : {(void *)scan_tmp, (void *)tot64}) {
+            cudaFree(q);
+            b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), q));
+        }
+        R0.padded = 1;
     }
     if (rowbound) {  // only needed for sizing
         cudaFree(rowbound);

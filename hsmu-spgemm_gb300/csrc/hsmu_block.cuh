@@ -19,7 +19,8 @@ __device__ __forceinline__ int seg_of(int incl, int g) {
     return s;
 }
 
-// Visit every B tile of the rows referenced by A entries [a_lo, a_hi), with
+// Visit every B tile of the rows referenced by A entries [a_lo, a_hi) (row k:
+// tiles tptr[k] .. tend[k]-1; tend = tptr + 1 for a CSR-style pointer array), with
 // the tile range of each B row optionally restricted to tile ids [c0, c1)
 // (RESTRICT: lower_bound on the sorted tile ids).  The A entries are taken
 // 32 at a time (one per lane: segment = that entry's B tile range); the flat
@@ -31,7 +32,8 @@ __device__ __forceinline__ int seg_of(int incl, int g) {
 template <bool RESTRICT, bool NC = true, class Fn>
 __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, int stride,
                                                 const int *__restrict__ acol, const int *__restrict__ tptr,
-                                                const int *__restrict__ tcol, int c0, int c1, Fn fn) {
+                                                const int *__restrict__ tend, const int *__restrict__ tcol, int c0,
+                                                int c1, Fn fn) {
     const int lane = lane_id();
     for (int pb = a_lo; pb < a_hi; pb += WARP) {
         const int p = pb + lane;
@@ -39,7 +41,7 @@ __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, i
         if (p < a_hi) {
             const int k = ldx<NC>(acol + p);
             lo = ldx<NC>(tptr + k);
-            hi = ldx<NC>(tptr + k + 1);
+            hi = ldx<NC>(tend + k);
             if (RESTRICT) {
                 lo = lower_bound_i32(tcol, lo, hi, c0);
                 hi = lower_bound_i32(tcol, lo, hi, c1);

@@ -13,6 +13,10 @@
 //
 // The per-thread lists live in shared memory laid out element-major
 // ([TINY_MAX][threads]) so that neighbouring threads hit neighbouring banks.
+//
+// B's row k is given as entries brp[k] .. bre[k]-1: bre = brp + 1 for a CSR
+// row pointer; the batched engine's intermediate rows (A*P of a Galerkin
+// product) sit in padded slots and have their own end array.
 #pragma once
 #include "hsmu_products.cuh"
 
@@ -33,7 +37,8 @@ struct TinyFetch {
 
     __device__ __forceinline__ void load(int p0, int a_hi, const int *__restrict__ acol,
                                          const double *__restrict__ aval, const int *__restrict__ brp,
-                                         const int *__restrict__ bcol, const double *__restrict__ bval) {
+                                         const int *__restrict__ bre, const int *__restrict__ bcol,
+                                         const double *__restrict__ bval) {
         int k[TINY_BATCH];
 #pragma unroll
         for (int u = 0; u < TINY_BATCH; u++) {
@@ -45,7 +50,7 @@ struct TinyFetch {
             qs[u] = qe[u] = 0;
             if (k[u] >= 0) {
                 qs[u] = ldx<NC>(brp + k[u]);
-                qe[u] = ldx<NC>(brp + k[u] + 1);
+                qe[u] = ldx<NC>(bre + k[u]);
             }
         }
 #pragma unroll
@@ -64,7 +69,7 @@ struct TinyFetch {
 // TINY_BATCH A entries per round of independent loads
 template <bool NC = true>
 __device__ __forceinline__ int tiny_products(int a_lo, int a_hi, const int *__restrict__ acol,
-                                             const int *__restrict__ brp, int limit) {
+                                             const int *__restrict__ brp, const int *__restrict__ bre, int limit) {
     int prod = 0;
     for (int p0 = a_lo; p0 < a_hi && prod <= limit; p0 += TINY_BATCH) {
         int k[TINY_BATCH];
@@ -72,7 +77,7 @@ __device__ __forceinline__ int tiny_products(int a_lo, int a_hi, const int *__re
         for (int u = 0; u < TINY_BATCH; u++) k[u] = p0 + u < a_hi ? ldx<NC>(acol + p0 + u) : -1;
 #pragma unroll
         for (int u = 0; u < TINY_BATCH; u++)
-            if (k[u] >= 0) prod += ldx<NC>(brp + k[u] + 1) - ldx<NC>(brp + k[u]);
+            if (k[u] >= 0) prod += ldx<NC>(bre + k[u]) - ldx<NC>(brp + k[u]);
     }
     return prod;
 }
@@ -81,12 +86,12 @@ __device__ __forceinline__ int tiny_products(int a_lo, int a_hi, const int *__re
 // more than TINY_MAX products (caller classified it wrongly).
 template <bool NC = true>
 __device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__restrict__ acol,
-                                              const int *__restrict__ brp, const int *__restrict__ bcol, int *cols,
-                                              int stride) {
+                                              const int *__restrict__ brp, const int *__restrict__ bre,
+                                              const int *__restrict__ bcol, int *cols, int stride) {
     int n = 0, seen = 0;
     for (int p0 = a_lo; p0 < a_hi; p0 += TINY_BATCH) {
         TinyFetch<NC, false> F;
-        F.load(p0, a_hi, acol, nullptr, brp, bcol, nullptr);
+        F.load(p0, a_hi, acol, nullptr, brp, bre, bcol, nullptr);
 #pragma unroll
         for (int u = 0; u < TINY_BATCH; u++) {
             for (int q = F.qs[u]; q < F.qe[u]; q++) {
@@ -110,13 +115,14 @@ __device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__r
 template <int AR, bool NC = true>
 __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
                                              const double *__restrict__ aval, const int *__restrict__ brp,
-                                             const int *__restrict__ bcol, const double *__restrict__ bval,
-                                             int *cols, double *acc, int stride, int cap, int *__restrict__ out_col,
+                                             const int *__restrict__ bre, const int *__restrict__ bcol,
+                                             const double *__restrict__ bval, int *cols, double *acc, int stride,
+                                             int cap, int *__restrict__ out_col,
                                              double *__restrict__ out_val) {
     int n = 0, seen = 0;
     for (int p0 = a_lo; p0 < a_hi; p0 += TINY_BATCH) {
         TinyFetch<NC, true> F;
-        F.load(p0, a_hi, acol, aval, brp, bcol, bval);
+        F.load(p0, a_hi, acol, aval, brp, bre, bcol, bval);
 #pragma unroll
         for (int u = 0; u < TINY_BATCH; u++) {
             const double a = F.a[u];
@@ -159,14 +165,14 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
 // last entries of the referenced (sorted) B rows; returns products too.
 template <bool NC = true>
 __device__ __forceinline__ void warp_row_extent(int a_lo, int a_hi, const int *__restrict__ acol,
-                                                const int *__restrict__ brp, const int *__restrict__ bcol,
-                                                int &cmin, int &cmax, int &prod) {
+                                                const int *__restrict__ brp, const int *__restrict__ bre,
+                                                const int *__restrict__ bcol, int &cmin, int &cmax, int &prod) {
     cmin = 0x7fffffff;
     cmax = -1;
     prod = 0;
     for (int p = a_lo + lane_id(); p < a_hi; p += WARP) {
         const int k = ldx<NC>(acol + p);
-        const int s = ldx<NC>(brp + k), e = ldx<NC>(brp + k + 1);
+        const int s = ldx<NC>(brp + k), e = ldx<NC>(bre + k);
         if (e > s) {
             cmin = min(cmin, ldx<NC>(bcol + s));
             cmax = max(cmax, ldx<NC>(bcol + e - 1));
@@ -184,12 +190,13 @@ __device__ __forceinline__ void warp_row_extent(int a_lo, int a_hi, const int *_
 // OR the row's columns into msk[0..span) (tile t0 + i at msk[i]); false on a column outside the span
 template <bool NC = true>
 __device__ __forceinline__ bool warp_row_masks(int a_lo, int a_hi, const int *__restrict__ acol,
-                                               const int *__restrict__ brp, const int *__restrict__ bcol, int t0,
+                                               const int *__restrict__ brp, const int *__restrict__ bre,
+                                               const int *__restrict__ bcol, int t0,
                                                int span, unsigned long long *msk) {
     for (int t = lane_id(); t < span; t += WARP) msk[t] = 0ull;
     __syncwarp();
     bool bad = false;
-    warp_walk_tiles<false, NC>(a_lo, a_hi, 0, WARP, acol, brp, bcol, 0, 0, [&](int q) {
+    warp_walk_tiles<false, NC>(a_lo, a_hi, 0, WARP, acol, brp, bre, bcol, 0, 0, [&](int q) {
         const int j = ldx<NC>(bcol + q);
         const int t = (j >> 6) - t0;
         if (t >= 0 && t < span) smem_setbit64(msk + t, j & 63);
@@ -212,8 +219,8 @@ __device__ __forceinline__ int warp_mask_count(const unsigned long long *msk, in
 template <int AR, bool NC = true>
 __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
                                               const double *__restrict__ aval, const int *__restrict__ brp,
-                                              const int *__restrict__ bcol, const double *__restrict__ bval,
-                                              int t0, int span, const unsigned long long *msk, int *base,
+                                              const int *__restrict__ bre, const int *__restrict__ bcol,
+                                              const double *__restrict__ bval, int t0, int span, const unsigned long long *msk, int *base,
                                               double *acc, int nnz, int *__restrict__ out_col,
                                               double *__restrict__ out_val) {
     const int lane = lane_id();
@@ -239,7 +246,7 @@ __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__r
     __syncwarp();
     auto seg = [&](int, int k, int &elo, int &ehi) {
         elo = ldx<NC>(brp + k);
-        ehi = ldx<NC>(brp + k + 1);
+        ehi = ldx<NC>(bre + k);
     };
     auto lookup = [&](int j) -> int {
         const int t = (j >> 6) - t0;

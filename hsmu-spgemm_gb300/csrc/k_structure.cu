@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
         if (skip_row(out, i)) continue;
         const long long c0 = out_base(out, i);
         const int lim = out_limit(out, i);
-        const int got = tiny_row_fill<AR>(arp[i], arp[i + 1], acol, aval, brp, bcol, bval, s_cols + threadIdx.x,
+        const int got = tiny_row_fill<AR>(arp[i], arp[i + 1], acol, aval, brp, brp + 1, bcol, bval, s_cols + threadIdx.x,
                                           s_acc + threadIdx.x, TINYF_THREADS, lim, out.ccol + c0, out.cval + c0);
         if (out.mode == OUT_SPEC) {
             out.cnnz[i] = got < 0 ? 0 : got;

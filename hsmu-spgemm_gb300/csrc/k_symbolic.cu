@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(TINY_THREADS) k_count_tiny(int M, const int *_
     bool bad = false;
     for (int r = blockIdx.x * TINY_THREADS + threadIdx.x; r < n; r += gridDim.x * TINY_THREADS) {
         const int i = rows[r];
-        const int c = tiny_row_count(arp[i], arp[i + 1], acol, brp, bcol, s_cols + threadIdx.x, TINY_THREADS);
+        const int c = tiny_row_count(arp[i], arp[i + 1], acol, brp, brp + 1, bcol, s_cols + threadIdx.x, TINY_THREADS);
         if (c < 0) bad = true;
         ri.cnnz[i] = c < 0 ? 0 : c;
     }
