@@ -111,6 +111,35 @@ def test_galerkin_batch_fma_mode(engine):
         assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
 
 
+@pytest.mark.parametrize("tiny", [0, 16, 32])
+def test_galerkin_batch_wide_intermediate_rows(engine, tiny):
+    # A*P rows with up to ~60 products: the intermediate round's rows go through
+    # the warp path as well as the thread path (tiny 0: every row through the warp path)
+    import hsmu_gb
+
+    cases = [(1500, 40.0, 200, 1), (800, 25.0, 90, 2), (64, 3.0, 10, 3)]
+    As, Ps, Pts, host_ops = [], [], [], []
+    for n, lam, nc, seed in cases:
+        A = gen.poisson_random(n, lam, seed=seed)
+        P = gen.poisson_random(n, 1.5, seed=seed + 100, ncols=nc)
+        Pt = gen.transpose(P)
+        host_ops.append((A, P, Pt))
+        As.append(hsmu_gb.DeviceCSR.from_host(A))
+        Ps.append(hsmu_gb.DeviceCSR.from_host(P))
+        Pts.append(hsmu_gb.DeviceCSR.from_host(Pt))
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_GALERKIN, As, Ps, Pts)
+    b.set_params(tiny)
+    for _ in range(2):  # the padded intermediate is rewritten on every launch
+        b.execute()
+        b.status()
+        for p, (A, P, Pt) in enumerate(host_ops):
+            C = host(b.result(p))
+            rp, col, val = galerkin_oracle(A, P, Pt)
+            np.testing.assert_array_equal(C.row_ptr, rp.astype(np.int32))
+            np.testing.assert_array_equal(C.col, col)
+            assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
+
+
 def test_batch_reports_unsupported_rows(engine):
     import hsmu_gb
 
