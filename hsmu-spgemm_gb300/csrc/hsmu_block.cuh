@@ -68,7 +68,13 @@ __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, i
 // so a warp keeps OR_U L2 round trips in flight instead of one.
 constexpr int OR_U = 4;
 
-template <bool RESTRICT>
+// PACKED: the non-empty tile ranges of a group of A entries are packed into
+// lanes 0..nseg-1 (flat start st, index shift d = lo - st) and every step finds
+// the range of each item from the starts that fall inside it (one ballot and
+// one OR-reduction) instead of a shuffle search.  It pays off where a group
+// holds many short ranges (power-law rows, many steps per group); for groups
+// of a few steps (stencil rows) the packing costs more than it saves.
+template <bool RESTRICT, bool PACKED = false>
 __device__ __forceinline__ void warp_or_tiles(int a_lo, int a_hi, int first, int stride,
                                               const int *__restrict__ acol, const int *__restrict__ tptr,
                                               const int *__restrict__ tcol,
@@ -90,15 +96,34 @@ __device__ __forceinline__ void warp_or_tiles(int a_lo, int a_hi, int first, int
         const int n = hi - lo;
         const int incl = warp_incl_scan(n);
         const int total = __shfl_sync(FULL, incl, WARP - 1);
+        if (total == 0) continue;
         const int excl = incl - n;
+        int c_st = 0, c_d = 0;
+        if (PACKED) {
+            const unsigned ne = __ballot_sync(FULL, n > 0);
+            const int nseg = __popc(ne);
+            const int src = nth_set_bit(ne, min(lane, nseg - 1));
+            const int st_src = __shfl_sync(FULL, excl, src);
+            c_d = __shfl_sync(FULL, lo - excl, src);
+            c_st = lane < nseg ? st_src : INT_MAX;
+        }
         for (int f = first; f < total; f += stride * OR_U) {
             int tt[OR_U];
             unsigned long long mm[OR_U];
 #pragma unroll
             for (int u = 0; u < OR_U; u++) {
-                const int g = f + u * stride + lane;
-                const int s = seg_of(incl, g);
-                const int idx = __shfl_sync(FULL, lo, s) + (g - __shfl_sync(FULL, excl, s));
+                const int fu = f + u * stride;
+                const int g = fu + lane;
+                int idx;
+                if (PACKED) {
+                    const int before = __popc(__ballot_sync(FULL, c_st < fu));
+                    const unsigned rel = (unsigned)(c_st - fu);
+                    const unsigned sm = __reduce_or_sync(FULL, rel < 32u ? 1u << rel : 0u);
+                    idx = g + __shfl_sync(FULL, c_d, before + __popc(sm & lanemask_le()) - 1);
+                } else {
+                    const int s = seg_of(incl, g);
+                    idx = __shfl_sync(FULL, lo, s) + (g - __shfl_sync(FULL, excl, s));
+                }
                 tt[u] = INT_MIN;
                 mm[u] = 0ull;
                 if (g < total) {

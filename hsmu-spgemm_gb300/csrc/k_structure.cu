@@ -297,9 +297,9 @@ __global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__res
             __syncthreads();
             bool bad = false;
             if (one_chunk)
-                warp_or_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, len, S.msk, bad);
+                warp_or_tiles<false, true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, len, S.msk, bad);
             else
-                warp_or_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, len, S.msk, bad);
+                warp_or_tiles<true, true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, len, S.msk, bad);
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
             const int lo = min(len, (int)threadIdx.x * SL_PER), hi = min(len, lo + SL_PER);

@@ -85,9 +85,9 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
             __syncthreads();
             bool bad = false;
             if (one_chunk)
-                warp_or_tiles<false>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
+                warp_or_tiles<false, true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
             else
-                warp_or_tiles<true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
+                warp_or_tiles<true, true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
             int cnt = 0;
