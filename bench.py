@@ -57,12 +57,12 @@ class HostCSR:
 ARITH = {"rn": 0, "fma": 1, "imul": 2}
 
 TRAFFIC = {
-    # profiles/k_struct_ds_stencil27_32_dof3.md: 445.8 MB on the 32^3 case, scaled by the
+    # profiles/k_struct_ds_stencil27_32_dof3.md: 445.5 MB on the 32^3 case, scaled by the
     # algorithmic bytes (x1.993) to the 40^3 workload
-    "stencil27_40_dof3_AA": 888.5e6,
-    # profiles/k_numeric_rmat16_AA.md: 2.078 GB on R-MAT scale 16, scaled by the algorithmic
+    "stencil27_40_dof3_AA": 887.9e6,
+    # profiles/k_numeric_rmat16_AA.md: 2.079 GB on R-MAT scale 16, scaled by the algorithmic
     # bytes (x7.73) to scale 18
-    "rmat18_AA": 16.06e9,
+    "rmat18_AA": 16.07e9,
 }
 
 WORKLOADS = {
