@@ -63,6 +63,10 @@ TRAFFIC = {
     # profiles/k_numeric_rmat16_AA.md: 2.079 GB on R-MAT scale 16, scaled by the algorithmic
     # bytes (x7.73) to scale 18
     "rmat18_AA": 16.07e9,
+    # profiles/k_batch_amg32_galerkin.md: 5.37 GB per launch of the 32-product batch (tuned
+    # launch); the 512-product batch scaled by its algorithmic bytes (x11.82)
+    "amg32_galerkin": 5.37e9,
+    "amg512_galerkin": 63.5e9,
 }
 
 WORKLOADS = {
@@ -491,7 +495,7 @@ def run_batched(args):
         "roofline": {"bound": "hbm", "kernel": "k_batch (persistent: both products, count + scan + fill)",
                      "achieved": round(alg[0] / (ms * 1e-3) / 1e9, 2), "peak": load_peaks()[0], "unit": "GB/s",
                      "frac": round(alg[0] / (ms * 1e-3) / 1e9 / load_peaks()[0], 4), "peak_kind": load_peaks()[1],
-                     "traffic": None, "alg_bytes": alg[0]},
+                     "traffic": TRAFFIC.get(args.workload), "alg_bytes": alg[0]},
         "batched": {"ms": round(ms, 4), "plain_calls_ms": round(plain_ms, 3), "plain_calls": 2 * len(sides),
                     "speedup_vs_plain": round(plain_ms / ms, 2), "autotuned": {"tiny": tiny, "grid": grid},
                     "launches_per_step": 1, "graph": True},
