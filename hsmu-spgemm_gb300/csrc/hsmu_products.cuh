@@ -10,14 +10,19 @@
 //
 // The A entries are taken 32 at a time (one per lane); seg(p) gives the B
 // entry range [elo, ehi) that A entry p contributes to this accumulator.
-//   * long B segments (average >= 32 entries): one segment at a time, in
-//     chunks of up to LU steps of 32 entries.  Entries of one B row have
-//     distinct columns, so a chunk has no slot conflicts and only a change
-//     of segment needs a warp sync.  The next chunk's B loads are issued
-//     before the current chunk's multiply/lookup/add (software pipeline).
-//   * short B segments: the flat sequence of (A entry, B entry) items, 32 per
-//     step; lanes that hit the same slot in one step (__match_any_sync) add in
-//     lane order = A-entry order.
+//   * long B segments (average >= LONG_SEG_MIN entries; callers may turn this
+//     path off): one segment at a time, in chunks of up to LU steps of 32
+//     entries.  Entries of one B row have distinct columns, so a chunk has no
+//     slot conflicts and only a change of segment needs a warp sync.  The
+//     next chunk's B loads are issued before the current chunk's
+//     multiply/lookup/add (software pipeline).
+//   * otherwise: the flat sequence of (A entry, B entry) items, 32 per step.
+//     The non-empty segments are packed into lanes; one OR-reduction per step
+//     marks the segment starts inside it, so every lane gets its segment from
+//     a popcount.  A step inside one segment has distinct slots; lanes of a
+//     step spanning several segments that hit the same slot add in lane order
+//     = A-entry order (found by __match_any_sync, or with TAG by stamping lane
+//     ids into a byte per slot and matching only the lanes that collide).
 #pragma once
 #include "hsmu_block.cuh"
 #include "hsmu_dmul.cuh"
