@@ -182,6 +182,9 @@ struct PlainRun {
     WinCursors wc{};
     int *crp = nullptr, *ccol = nullptr;
     double *cval = nullptr;
+    // caller-owned column/value arrays (int64 path: the panel's place in C); not freed here
+    int *ext_col = nullptr;
+    double *ext_val = nullptr;
     Ctl *ctl = nullptr;
     Ctl hc{};
     int launches = 0;
@@ -247,8 +250,13 @@ struct PlainRun {
     }
 
     int alloc_output() {
-        CKR(palloc(&ccol, (size_t)hc.nnz + COL_PAD, st));
-        CKR(palloc(&cval, (size_t)hc.nnz, st));
+        if (ext_col) {
+            ccol = ext_col;
+            cval = ext_val;
+        } else {
+            CKR(palloc(&ccol, (size_t)hc.nnz + COL_PAD, st));
+            CKR(palloc(&cval, (size_t)hc.nnz, st));
+        }
         CKR(palloc(&win, (size_t)win_cap, st));
         if (hc.bin_count[BIN_L] == 0 && hc.wide_rows == 0) return HSMU_OK;  // no windows
         return alloc_cursors(win_cap, (long long)hc.cur_bound);
@@ -310,8 +318,6 @@ struct PlainRun {
         pfree(ri.tmin, st);
         pfree(ri.tmax, st);
         pfree(ri.bins, st);
-    pfree(ri.cls, st);
-    pfree(ri.bin_cnt, st);
         pfree(ri.cls, st);
         pfree(ri.bin_cnt, st);
         pfree(ri.cnnz, st);
@@ -323,6 +329,10 @@ struct PlainRun {
         pfree(wc.scan_tmp, st);
         pfree(wc.cur, st);
         pfree(crp, st);
+        if (ext_col) {
+            ccol = nullptr;
+            cval = nullptr;
+        }
         pfree(ccol, st);
         pfree(cval, st);
     }
@@ -776,6 +786,99 @@ done:
     return rc;
 }
 
+// hsmu_spgemm64: exact nnz of every row, int64 row pointers (device scan, one host read of
+// them), then panels of consecutive rows whose entries fit int32, each run by the plain
+// engine straight into its place in C; B's tiles are built once for all panels
+int spgemm64_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr64 *C, long long max_panel,
+                  const hsmu_opts *opts, cudaStream_t st) {
+    if (!h || !csr_ok(A) || !csr_ok(B) || !C || A->N != B->M || max_panel < 0) return HSMU_ERR_INVALID;
+    hsmu_opts o{};
+    if (opts) o = *opts;
+    if (!arith_ok(o)) return HSMU_ERR_INVALID;
+    std::memset(C, 0, sizeof(*C));
+    const long long cap = (max_panel == 0 || max_panel > INT_MAX) ? INT_MAX : max_panel;
+    const int M = A->M;
+    int rc = HSMU_OK;
+    int *cnt = nullptr, *scan_tmp = nullptr, *col = nullptr;
+    long long *rp = nullptr, *tot = nullptr;
+    double *val = nullptr;
+    Ctl *ctl = nullptr;
+    hsmu_btiles bt{};
+    std::vector<long long> hrp;
+    hsmu_opts po = o;
+    po.validate = 0;  // the panels are views into A: the operands are checked once, here
+    if (o.validate) {
+        PlainRun v(h, st, o);
+        rc = v.begin(A, B);
+        v.release();
+        if (rc) goto done;
+    }
+    CK(palloc(&cnt, (size_t)M + 1, st));
+    rc = row_nnz_impl(h, A, B, cnt, st);
+    if (rc) goto done;
+    CK(palloc(&rp, (size_t)M + 1, st));
+    CK(palloc(&tot, 1, st));
+    CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
+    launch_scan64(cnt, rp, M, tot, scan_tmp, st);
+    CK(cudaGetLastError());
+    hrp.resize((size_t)M + 1);
+    CK(cudaMemcpyAsync(hrp.data(), rp, sizeof(long long) * ((size_t)M + 1), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(palloc(&col, (size_t)hrp[M] + COL_PAD, st));
+    CK(palloc(&val, (size_t)hrp[M], st));
+    CK(palloc(&ctl, 1, st));
+    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    rc = build_tiles(h, B, &bt, ctl, 0, st, true);
+    if (rc) goto done;
+    for (int r0 = 0; r0 < M;) {
+        // rows r0 .. r1-1: as many as keep the panel within the cap, at least one
+        int r1 = (int)(std::upper_bound(hrp.begin() + r0 + 1, hrp.end(), hrp[r0] + cap) - hrp.begin()) - 1;
+        if (r1 <= r0) r1 = r0 + 1;
+        hsmu_csr Ap = *A;
+        Ap.M = r1 - r0;
+        Ap.row_ptr = A->row_ptr + r0;
+        PlainRun r(h, st, po);
+        r.ext_col = col + hrp[r0];
+        r.ext_val = val + hrp[r0];
+        rc = r.begin(&Ap, B);
+        if (!rc) rc = r.symbolic(B, &bt, false, nullptr, nullptr);
+        if (!rc && r.hc.nnz != hrp[r1] - hrp[r0]) rc = HSMU_ERR_INTERNAL;
+        if (!rc) rc = r.alloc_output();
+        if (!rc) {
+            r.structure(0, Ap.M);
+            r.values();
+            rc = r.finish();
+        }
+        r.release();
+        if (rc) goto done;
+        r0 = r1;
+    }
+    C->M = M;
+    C->N = B->N;
+    C->nnz = hrp[M];
+    C->owned = 1;
+    C->row_ptr = reinterpret_cast<int64_t *>(rp);
+    C->col = col;
+    C->val = val;
+    rp = nullptr;
+    col = nullptr;
+    val = nullptr;
+done:
+    pfree(cnt, st);
+    pfree(scan_tmp, st);
+    pfree(tot, st);
+    pfree(ctl, st);
+    pfree(bt.tile_ptr, st);
+    pfree(bt.tile_col, st);
+    pfree(bt.mask, st);
+    pfree(bt.tile_off, st);
+    pfree(rp, st);
+    pfree(col, st);
+    pfree(val, st);
+    cudaStreamSynchronize(st);
+    return rc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -861,6 +964,22 @@ int hsmu_spgemm_tiled(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, const
 int hsmu_spgemm_learned(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
                         const hsmu_opts *opts, void *stream, hsmu_stats *stats) {
     return spgemm_learned_impl(h, A, B, C, model, opts, static_cast<cudaStream_t>(stream), stats);
+}
+
+int hsmu_spgemm64(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr64 *C, int64_t max_panel_nnz,
+                  const hsmu_opts *opts, void *stream) {
+    return spgemm64_impl(h, A, B, C, (long long)max_panel_nnz, opts, static_cast<cudaStream_t>(stream));
+}
+
+int hsmu_csr64_free(hsmu_csr64 *C) {
+    if (!C) return HSMU_ERR_INVALID;
+    if (C->owned) {
+        cudaFree(C->row_ptr);
+        cudaFree(C->col);
+        cudaFree(C->val);
+    }
+    std::memset(C, 0, sizeof(*C));
+    return HSMU_OK;
 }
 
 int hsmu_row_nnz(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, int32_t *nnz, void *stream) {
@@ -985,6 +1104,21 @@ int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int rc = HSMU_OK;
     CK(cudaMemcpyAsync(row_ptr, C->row_ptr, sizeof(int32_t) * ((size_t)C->M + 1), cudaMemcpyDeviceToHost, st));
+    if (C->nnz > 0) {
+        CK(cudaMemcpyAsync(col, C->col, sizeof(int32_t) * (size_t)C->nnz, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(val, C->val, sizeof(double) * (size_t)C->nnz, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+done:
+    return rc;
+}
+
+int hsmu_csr64_download(const hsmu_csr64 *C, int64_t *row_ptr, int32_t *col, double *val, void *stream) {
+    if (!C || C->M < 0 || C->nnz < 0 || !C->row_ptr || !row_ptr || (C->nnz > 0 && (!C->col || !C->val || !col || !val)))
+        return HSMU_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = HSMU_OK;
+    CK(cudaMemcpyAsync(row_ptr, C->row_ptr, sizeof(int64_t) * ((size_t)C->M + 1), cudaMemcpyDeviceToHost, st));
     if (C->nnz > 0) {
         CK(cudaMemcpyAsync(col, C->col, sizeof(int32_t) * (size_t)C->nnz, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(val, C->val, sizeof(double) * (size_t)C->nnz, cudaMemcpyDeviceToHost, st));

@@ -42,7 +42,8 @@ EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_hand
            "hsmu_batch_create", "hsmu_batch_execute", "hsmu_batch_graph_launch", "hsmu_batch_status",
            "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
            "hsmu_gen_poisson7", "hsmu_gen_aggregation", "hsmu_spgemm_learned", "hsmu_row_features",
-           "hsmu_row_nnz", "hsmu_mlp_forward", "hsmu_mlp_grad", "hsmu_mlp_adam"]
+           "hsmu_row_nnz", "hsmu_mlp_forward", "hsmu_mlp_grad", "hsmu_mlp_adam", "hsmu_spgemm64",
+           "hsmu_csr64_free", "hsmu_csr64_download"]
 MLP_FLOATS = 1259
 
 
@@ -56,6 +57,12 @@ class c_csr(ctypes.Structure):
     _fields_ = [("M", ctypes.c_int32), ("N", ctypes.c_int32), ("nnz", ctypes.c_int32),
                 ("owned", ctypes.c_int32), ("row_ptr", ctypes.c_void_p), ("col", ctypes.c_void_p),
                 ("val", ctypes.c_void_p)]
+
+
+class c_csr64(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int32), ("N", ctypes.c_int32), ("nnz", ctypes.c_int64),
+                ("owned", ctypes.c_int32), ("reserved", ctypes.c_int32), ("row_ptr", ctypes.c_void_p),
+                ("col", ctypes.c_void_p), ("val", ctypes.c_void_p)]
 
 
 class c_btiles(ctypes.Structure):
@@ -139,6 +146,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_mlp_grad.argtypes = [P, P, P, ctypes.c_int, P, P, P]
     L.hsmu_mlp_adam.argtypes = [P, P, P, P, ctypes.c_float, ctypes.c_float, ctypes.c_int, P]
     L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
+    L.hsmu_spgemm64.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr64),
+                                ctypes.c_int64, ctypes.POINTER(c_opts), P]
+    L.hsmu_csr64_free.argtypes = [ctypes.POINTER(c_csr64)]
+    L.hsmu_csr64_download.argtypes = [ctypes.POINTER(c_csr64), P, P, P, P]
     _lib = L
     return L
 
@@ -279,6 +290,44 @@ def _stream_ptr(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
+class DeviceCSR64:
+    """A library-owned CSR with int64 row pointers (output of hsmu_spgemm64)."""
+
+    def __init__(self, desc: c_csr64):
+        self.desc = desc
+
+    @property
+    def M(self):
+        return self.desc.M
+
+    @property
+    def N(self):
+        return self.desc.N
+
+    @property
+    def nnz(self):
+        return self.desc.nnz
+
+    def to_host(self, stream=None):
+        """(row_ptr int64, col int32, val float64) numpy arrays"""
+        rp = np.empty(self.M + 1, dtype=np.int64)
+        col = np.empty(self.nnz, dtype=np.int32)
+        val = np.empty(self.nnz, dtype=np.float64)
+        _check(load_library().hsmu_csr64_download(ctypes.byref(self.desc), rp.ctypes.data, col.ctypes.data,
+                                                  val.ctypes.data, _stream_ptr(stream)), "hsmu_csr64_download")
+        return rp, col, val
+
+    def free(self):
+        if self.desc.owned:
+            load_library().hsmu_csr64_free(ctypes.byref(self.desc))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 class Engine:
     """One library handle on the current CUDA device (hsmu_handle_create)."""
 
@@ -355,6 +404,17 @@ class Engine:
         _check(rc, "hsmu_spgemm")
         self.last_stats = st.as_dict() if stats else None
         return DeviceCSR(C)
+
+    def spgemm64(self, A: DeviceCSR, B: DeviceCSR, *, max_panel_nnz: int = 0, validate: bool = False,
+                 arith: int = 0, stream=None) -> "DeviceCSR64":
+        """C = A * B with int64 row pointers (hsmu_spgemm64): rows processed in panels of
+        at most max_panel_nnz entries (0: INT32_MAX), written into one C."""
+        L = load_library()
+        C = c_csr64()
+        o = c_opts(int(validate), int(arith), 0)
+        _check(L.hsmu_spgemm64(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc), ctypes.byref(C),
+                               int(max_panel_nnz), ctypes.byref(o), _stream_ptr(stream)), "hsmu_spgemm64")
+        return DeviceCSR64(C)
 
 
     def transpose(self, A: DeviceCSR, stream=None) -> DeviceCSR:

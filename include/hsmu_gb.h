@@ -169,6 +169,34 @@ int hsmu_spgemm_host(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_c
 
 int hsmu_btiles_build(hsmu_handle h, const hsmu_csr *B, hsmu_btiles *out, void *stream);
 
+/* CSR with 64-bit row pointers, for products with more than INT32_MAX
+ * entries.  The reference's index type is int throughout (index_t,
+ * inc/NHC_spgemm.h:13; NHC_CSR::nnz, :77), which caps C at 2^31 - 1 entries
+ * (hsmu_spgemm reports such products with HSMU_ERR_OVERFLOW). */
+typedef struct hsmu_csr64 {
+    int32_t M;
+    int32_t N;
+    int64_t nnz;
+    int32_t owned;
+    int32_t reserved;
+    int64_t *row_ptr; /* [M+1] */
+    int32_t *col;     /* [nnz] */
+    double *val;      /* [nnz] */
+} hsmu_csr64;
+
+/* C = A * B on the device with C in hsmu_csr64 form (row pointers int64,
+ * library-owned: free with hsmu_csr64_free).  Same results as hsmu_spgemm.
+ * The exact nnz of every row comes first; the rows of A are then processed
+ * in panels whose entries fit int32 (at most max_panel_nnz each, 0 = INT32_MAX;
+ * a row with more entries than the cap is a panel of its own), each written
+ * straight into its place in C.  B's tiles are built once for all panels.
+ * Synchronizes `stream` before returning. */
+int hsmu_spgemm64(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr64 *C, int64_t max_panel_nnz,
+                  const hsmu_opts *opts, void *stream);
+int hsmu_csr64_free(hsmu_csr64 *C);
+/* hsmu_csr_download for an hsmu_csr64 (row_ptr[M+1] int64, col/val[nnz]) */
+int hsmu_csr64_download(const hsmu_csr64 *C, int64_t *row_ptr, int32_t *col, double *val, void *stream);
+
 /* At = A^T on the device, every row of At in ascending column order (a stable
  * radix sort of A's entries by column).  At is owned by the library
  * (hsmu_csr_free).  A must be canonical CSR.  Replaces the host transpose the
