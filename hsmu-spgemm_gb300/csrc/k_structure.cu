@@ -95,6 +95,7 @@ __device__ __forceinline__ int out_limit(const RowOut &o, int i) {
 constexpr int SDS_WARPS = 4;
 constexpr int SDS_CTAS_PER_SM = 6;
 constexpr int SDS_WL = 64;     // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
+static_assert(SPAN_T * 64 / WIN_CUT + 1 < SDS_WL, "window list of a warp row");
 
 struct SdsSmem {
     unsigned long long msk[SPAN_T];
