@@ -277,8 +277,8 @@ struct PlainRun {
     void structure(int lo, int hi) {
         if (hc.nnz == 0) return;
         launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_PLAIN, crp, nullptr, ccol, cval, nullptr, nullptr, lo, hi}, win,
-                         win_cap, ctl, o.arith, h->nsm, st);
-        launches += 3;
+                         win_cap, ctl, o.arith, h->nsm, st, hc.bin_count);
+        for (int b = 0; b < NBIN; b++) launches += hc.bin_count[b] > 0;
     }
 
     // values of the windows made by the preceding structure() call (none unless a row

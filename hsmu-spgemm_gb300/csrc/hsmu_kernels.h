@@ -82,8 +82,10 @@ void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo 
 
 // k_structure.cu
 // writes C's columns and numeric windows; rows that fit one warp also get their values
+// class_rows: rows per class (BIN_*) when known on the host; kernels of empty classes are skipped
 void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
-                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st);
+                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st,
+                      const int *class_rows = nullptr);
 
 // k_numeric.cu
 // flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped;

@@ -429,14 +429,19 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
 }
 
 void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
-                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
-    auto kt = arith == AR_IMUL ? k_fill_tiny<AR_IMUL> : arith == AR_FMA ? k_fill_tiny<AR_FMA> : k_fill_tiny<AR_RN>;
-    kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, out, ctl);
-    auto kds = arith == AR_IMUL ? k_struct_ds<AR_IMUL> : arith == AR_FMA ? k_struct_ds<AR_FMA> : k_struct_ds<AR_RN>;
-    kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
-        A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
-    k_struct_l<<<nsm * 4, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
-                                                            win, win_cap, ctl);
+                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st, const int *class_rows) {
+    if (!class_rows || class_rows[BIN_TINY] > 0) {
+        auto kt = arith == AR_IMUL ? k_fill_tiny<AR_IMUL> : arith == AR_FMA ? k_fill_tiny<AR_FMA> : k_fill_tiny<AR_RN>;
+        kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, out, ctl);
+    }
+    if (!class_rows || class_rows[BIN_DS] > 0) {
+        auto kds = arith == AR_IMUL ? k_struct_ds<AR_IMUL> : arith == AR_FMA ? k_struct_ds<AR_FMA> : k_struct_ds<AR_RN>;
+        kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
+            A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
+    }
+    if (!class_rows || class_rows[BIN_L] > 0)
+        k_struct_l<<<nsm * 4, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
+                                                                win, win_cap, ctl);
 }
 
 int configure_structure() {
