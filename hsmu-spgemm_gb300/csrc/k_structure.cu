@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
     }
 }
 
-constexpr int SL_THREADS = 256;
+constexpr int SL_THREADS = 512;  // 16 warps per wide row, 3 CTAs per SM (40 registers)
 // > max windows in one chunk: DCH*64/WIN_CUT (slot cuts) + DCH/WIN_TCAP (rank cuts) + DCH/WIN_SPAN + 1
 constexpr int SL_WL = 512;
 constexpr int SL_PER = DCH_STRUCT / SL_THREADS;
@@ -263,7 +263,7 @@ struct SlSmem {
     int wt[SL_WL];
 };
 
-__global__ void __launch_bounds__(SL_THREADS) k_struct_l(int M, const int *__restrict__ arp,
+__global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__restrict__ arp,
                                                          const int *__restrict__ acol,
                                                          const int *__restrict__ tptr,
                                                          const int *__restrict__ tcol,
@@ -440,7 +440,7 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
             A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
     }
     if (!class_rows || class_rows[BIN_L] > 0)
-        k_struct_l<<<nsm * 4, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
+        k_struct_l<<<nsm * 3, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
                                                                 win, win_cap, ctl);
 }
 
