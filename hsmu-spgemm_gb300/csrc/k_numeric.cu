@@ -44,7 +44,7 @@ namespace hsmu {
 
 constexpr int NUM_WARPS = 3;
 constexpr int NUM_CTAS_PER_SM = 5;
-constexpr int GW = 4;  // consecutive windows per work item, handed out dynamically
+constexpr int GW = 2;  // consecutive windows per work item, handed out dynamically
 constexpr int STAGE_LIMIT = 1 << 20;  // polls of a column copy before the kernel reports a timeout
 
 // per warp; acc first: it also receives the window's columns by bulk copy
