@@ -54,14 +54,16 @@ def test_struct_layouts(tmp_path):
 
     prog = tmp_path / "sizes.c"
     prog.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "hsmu_gb.h"\n'
-                    'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(hsmu_csr), sizeof(hsmu_btiles),'
-                    ' sizeof(hsmu_opts), sizeof(hsmu_stats), offsetof(hsmu_stats, ms_convert),'
-                    ' offsetof(hsmu_stats, launches)); return 0;}\n')
+                    'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(hsmu_csr),'
+                    ' sizeof(hsmu_btiles), sizeof(hsmu_opts), sizeof(hsmu_stats), offsetof(hsmu_stats, ms_convert),'
+                    ' offsetof(hsmu_stats, launches), sizeof(hsmu_csr64), offsetof(hsmu_csr64, nnz),'
+                    ' offsetof(hsmu_csr64, row_ptr)); return 0;}\n')
     exe = str(tmp_path / "sizes")
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", exe])
     got = [int(x) for x in subprocess.check_output([exe]).split()]
     want = [ctypes.sizeof(hsmu_gb.c_csr), ctypes.sizeof(hsmu_gb.c_btiles), ctypes.sizeof(hsmu_gb.c_opts),
-            ctypes.sizeof(hsmu_gb.c_stats), hsmu_gb.c_stats.ms_convert.offset, hsmu_gb.c_stats.launches.offset]
+            ctypes.sizeof(hsmu_gb.c_stats), hsmu_gb.c_stats.ms_convert.offset, hsmu_gb.c_stats.launches.offset,
+            ctypes.sizeof(hsmu_gb.c_csr64), hsmu_gb.c_csr64.nnz.offset, hsmu_gb.c_csr64.row_ptr.offset]
     assert got == want
 
 
