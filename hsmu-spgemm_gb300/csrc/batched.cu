@@ -90,9 +90,10 @@ struct BParams {
     GridBar *bar;
     int *err;
     int arith;             // hsmu_opts.arith of the batch
+    unsigned long long spin_limit;  // polls of a grid barrier before it gives up
 };
 
-__device__ bool grid_sync(GridBar *gb, int *err) {
+__device__ bool grid_sync(GridBar *gb, int *err, unsigned long long spin_limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -108,7 +109,7 @@ __device__ bool grid_sync(GridBar *gb, int *err) {
         } else {
             unsigned long long it = 0;
             while (*vgen == g) {
-                if (++it > SPIN_LIMIT) {
+                if (++it > spin_limit) {
                     atomicOr(err, BERR_TIMEOUT);
                     ok = 0;
                     break;
@@ -295,7 +296,7 @@ __device__ bool phase_scan(const BParams &P, int r) {
     long long tot;
     block_excl_sum<BW * 32>(v, s_tmp, tot);
     if (threadIdx.x == 0) P.bsum[blockIdx.x] = tot;
-    if (!grid_sync(P.bar, P.err)) return false;
+    if (!grid_sync(P.bar, P.err, P.spin_limit)) return false;
     if (blockIdx.x == 0) {
         long long carry = 0;
         for (int b0 = 0; b0 < (int)gridDim.x; b0 += blockDim.x) {
@@ -312,7 +313,7 @@ __device__ bool phase_scan(const BParams &P, int r) {
             if (carry > R.cap) atomicOr(P.err, BERR_CAPACITY);
         }
     }
-    if (!grid_sync(P.bar, P.err)) return false;
+    if (!grid_sync(P.bar, P.err, P.spin_limit)) return false;
     // block scan of the chunk, in tiles of SCAN_RUN rows per thread (one block scan,
     // three barriers, per tile of blockDim * SCAN_RUN rows)
     constexpr int SCAN_RUN = 16;
@@ -358,16 +359,16 @@ __global__ void __launch_bounds__(BW * 32) k_batch(BParams P) {
     extern __shared__ unsigned long long s_dyn[];
     BWarpSmem &S = reinterpret_cast<BWarpSmem *>(s_dyn)[threadIdx.x >> 5];
     for (int r = 0; r < P.nrounds; r++) {
-        if (r > 0 && !grid_sync(P.bar, P.err)) return;
+        if (r > 0 && !grid_sync(P.bar, P.err, P.spin_limit)) return;
         if (P.rnd[r].padded) {  // only round 0 (operands from the caller) is ever padded
             phase_rows<AR, RM_PADDED, true>(P, r, S);
             continue;
         }
         if (r == 0) phase_rows<AR, RM_COUNT, true>(P, r, S);
         else phase_rows<AR, RM_COUNT, false>(P, r, S);
-        if (!grid_sync(P.bar, P.err)) return;
+        if (!grid_sync(P.bar, P.err, P.spin_limit)) return;
         if (!phase_scan(P, r)) return;
-        if (!grid_sync(P.bar, P.err)) return;
+        if (!grid_sync(P.bar, P.err, P.spin_limit)) return;
         if (*(volatile int *)P.err & BERR_CAPACITY) return;
         phase_rowptr(P, r);
         if (r == 0) phase_rows<AR, RM_FILL, true>(P, r, S);
@@ -514,6 +515,8 @@ int hsmu_batch_create(hsmu_handle h, int kind, int n, const hsmu_csr *A, const h
     b->kind = kind;
     b->nprod = n;
     b->arith = opts ? opts->arith : AR_RN;
+    // test hook: barriers that give up after opts->wait_polls spins
+    b->P.spin_limit = (opts && opts->wait_polls > 0) ? (unsigned long long)opts->wait_polls : SPIN_LIMIT;
     b->tiny = TINY_MAX;
     int dev = 0;
     cudaGetDevice(&dev);

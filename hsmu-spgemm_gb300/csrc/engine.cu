@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -28,6 +29,14 @@
 
 namespace hsmu {
 int configure_count();
+
+int status_from_dev_err(int err) {
+    if (!err) return HSMU_OK;
+    if (err & DERR_UNSORTED) return HSMU_ERR_UNSORTED;
+    if (err & DERR_OVERFLOW) return HSMU_ERR_OVERFLOW;
+    if (err & DERR_TIMEOUT) return HSMU_ERR_TIMEOUT;
+    return HSMU_ERR_INTERNAL;
+}
 int configure_structure();
 int configure_numeric();
 }  // namespace hsmu
@@ -38,6 +47,8 @@ struct hsmu_handle_s {
     int device;
     int nsm;
     Ctl *h_ctl;  // pinned host mirror of the control block
+    Ctl *h_mid;  // pinned mirror read after the bounds pass (tile store size)
+    cudaEvent_t ev_mid;
     cudaEvent_t ev[8];
     // host-buffer entry: copy streams and their ordering events
     cudaStream_t cs_in, cs_out;
@@ -80,17 +91,14 @@ int from_cuda(cudaError_t e) {
         }                                    \
     } while (0)
 
-int err_from_dev(int err) {
-    if (!err) return HSMU_OK;
-    if (err & DERR_UNSORTED) return HSMU_ERR_UNSORTED;
-    if (err & DERR_OVERFLOW) return HSMU_ERR_OVERFLOW;
-    if (err & DERR_TIMEOUT) return HSMU_ERR_TIMEOUT;
-    return HSMU_ERR_INTERNAL;
-}
+int err_from_dev(int err) { return status_from_dev_err(err); }
 
 // C's column array: 4 ints of slack past nnz, so that the value pass can fetch a
 // window's columns in 16-byte units with bulk copies
 constexpr size_t COL_PAD = 4;
+// largest tile store (12 bytes per tile: 16 GB); beyond it the structure pass
+// repeats the large rows' OR walk instead
+constexpr long long STORE_MAX_TILES = (16ll << 30) / 12;
 
 bool csr_ok(const hsmu_csr *X) {
     if (!X || X->M < 0 || X->N < 0 || X->nnz < 0) return false;
@@ -101,10 +109,17 @@ bool csr_ok(const hsmu_csr *X) {
 
 DevCSR dev(const hsmu_csr *X) { return DevCSR{X->M, X->N, (long long)X->nnz, X->row_ptr, X->col, X->val}; }
 
+// allocation-failure injection (hsmu_debug_fail_alloc): the countdown reaches 0
+// at the allocation that is made to fail; 0 = disarmed
+std::atomic<long long> g_fail_alloc_countdown{0};
+
 template <class T>
 cudaError_t palloc(T **p, size_t n, cudaStream_t st) {
     *p = nullptr;
     if (n == 0) n = 1;
+    if (g_fail_alloc_countdown.load(std::memory_order_relaxed) > 0 &&
+        g_fail_alloc_countdown.fetch_sub(1, std::memory_order_relaxed) == 1)
+        return cudaErrorMemoryAllocation;
     return cudaMallocAsync(reinterpret_cast<void **>(p), n * sizeof(T), st);
 }
 
@@ -148,7 +163,13 @@ done:
     pfree(tcnt, st);
     pfree(scan_tmp, st);
     pfree(tot, st);
-    if (rc != HSMU_OK) hsmu_btiles_free(out);
+    if (rc != HSMU_OK) {
+        // stream-ordered allocations go back the same way
+        pfree(out->tile_ptr, st);
+        pfree(out->tile_col, st);
+        pfree(out->mask, st);
+        pfree(out->tile_off, st);
+    }
     return rc;
 }
 
@@ -188,6 +209,11 @@ struct PlainRun {
     Ctl *ctl = nullptr;
     Ctl hc{};
     int launches = 0;
+    // C tiles of the large rows, kept by the count pass for the structure pass
+    long long *ts_off = nullptr;
+    int *ts_cnt = nullptr, *ts_col = nullptr;
+    unsigned long long *ts_mask = nullptr;
+    bool have_store = false;
 
     PlainRun(hsmu_handle_s *h_, cudaStream_t st_, const hsmu_opts &o_) : h(h_), st(st_), o(o_) {}
     ~PlainRun() { release(); }
@@ -214,6 +240,16 @@ struct PlainRun {
     // host_rp != NULL: the row pointers of C are copied there in the same host read
     int symbolic(const hsmu_csr *B, const hsmu_btiles *Bt_in, bool count_tiles, int32_t *host_rp,
                  cudaEvent_t ev_tiles) {
+        int rc = tiles_bounds(B, Bt_in, count_tiles, ev_tiles, o.no_tile_store == 0);
+        if (!rc) rc = count_scan(host_rp);
+        return rc;
+    }
+
+    // B's tiles (built, or the caller's) and the bounds pass: products, tile span and class
+    // of every row of A, the class bins; with `store`, also the tile store's row offsets,
+    // whose total is read back (overlapped with the next kernels) by count_scan
+    int tiles_bounds(const hsmu_csr *B, const hsmu_btiles *Bt_in, bool count_tiles, cudaEvent_t ev_tiles,
+                     bool store) {
         if (Bt_in) {
             bt = *Bt_in;
         } else {
@@ -232,11 +268,45 @@ struct PlainRun {
         CKR(palloc(&ri.bin_cnt, bin_scratch_ints(M), st));
         CKR(palloc(&ri.cnnz, (size_t)M + 1, st));
         CKR(palloc(&scan_tmp, scan_tmp_ints(M), st));
-        CKR(palloc(&crp, (size_t)M + 1, st));
+        if (store) {
+            CKR(palloc(&ri.tcap, (size_t)M, st));
+            CKR(palloc(&ts_off, (size_t)M + 1, st));
+        }
         launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
-        launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
+        launches += 6;  // bounds + binning
+        if (store) {
+            launch_scan64(ri.tcap, ts_off, M, &ctl->store_tiles, scan_tmp, st);
+            launches += 3;
+            CKR(cudaMemcpyAsync(h->h_mid, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+            CKR(cudaEventRecord(h->ev_mid, st));
+        }
+        CKR(cudaGetLastError());
+        return HSMU_OK;
+    }
+
+    // exact count of every row (the large rows' tiles kept in the store when it fits),
+    // scan into C's row pointers and nnz(C), one host read
+    int count_scan(int32_t *host_rp) {
+        CKR(palloc(&crp, (size_t)M + 1, st));
+        launch_count_small(Ad, Bd, Btd, ri, ctl, h->nsm, st);
+        launches += 2;
+        TileStore tsd{};
+        if (ri.tcap) {
+            // bounds are done once ev_mid has passed; the small rows' count runs meanwhile
+            CKR(cudaEventSynchronize(h->ev_mid));
+            const Ctl m = *h->h_mid;
+            if (m.err) return err_from_dev(m.err);
+            if (m.bin_count[BIN_L] > 0 && m.store_tiles > 0 && m.store_tiles <= STORE_MAX_TILES) {
+                CKR(palloc(&ts_cnt, (size_t)M, st));
+                CKR(palloc(&ts_col, (size_t)m.store_tiles, st));
+                CKR(palloc(&ts_mask, (size_t)m.store_tiles, st));
+                tsd = TileStore{ts_off, ts_cnt, ts_col, ts_mask};
+                have_store = true;
+            }
+        }
+        launch_count_large(Ad, Btd, ri, have_store ? &tsd : nullptr, ctl, h->nsm, st);
         launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
-        launches += 12;  // bounds + binning 6, count 3, scan 3
+        launches += 4;  // large-row count, scan 3
         CKR(cudaGetLastError());
         CKR(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
         if (host_rp) CKR(cudaMemcpyAsync(host_rp, crp, sizeof(int32_t) * ((size_t)M + 1), cudaMemcpyDeviceToHost, st));
@@ -276,8 +346,9 @@ struct PlainRun {
     // sorted columns of rows lo..hi-1, values of warp-sized rows, numeric windows of the others
     void structure(int lo, int hi) {
         if (hc.nnz == 0) return;
+        const TileStore tsd{ts_off, ts_cnt, ts_col, ts_mask};
         launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_PLAIN, crp, nullptr, ccol, cval, nullptr, nullptr, lo, hi}, win,
-                         win_cap, ctl, o.arith, h->nsm, st, hc.bin_count);
+                         win_cap, ctl, o.arith, h->nsm, st, hc.bin_count, have_store ? &tsd : nullptr);
         for (int b = 0; b < NBIN; b++) launches += hc.bin_count[b] > 0;
     }
 
@@ -286,7 +357,7 @@ struct PlainRun {
     void values() {
         if (hc.nnz == 0 || win_cap == 0 || (hc.bin_count[BIN_L] == 0 && hc.wide_rows == 0)) return;
         launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, wc, ctl, o.arith, h->nsm,
-                       st);
+                       st, o.wait_polls);
         launches += 6;  // window lengths, 3 scan, cursors, values
     }
 
@@ -321,6 +392,12 @@ struct PlainRun {
         pfree(ri.cls, st);
         pfree(ri.bin_cnt, st);
         pfree(ri.cnnz, st);
+        pfree(ri.tcap, st);
+        pfree(ts_off, st);
+        pfree(ts_cnt, st);
+        pfree(ts_col, st);
+        pfree(ts_mask, st);
+        have_store = false;
         pfree(scan_tmp, st);
         pfree(win, st);
         pfree(wc.len, st);
@@ -543,6 +620,12 @@ done:
 }
 
 // Learned path (see learned.cu): predicted slots instead of the exact count pass.
+// B's tiles and the bounds pass are shared with the plain path (a PlainRun holds
+// them); one host read after the bounds pass decides the route: an input with no
+// row of the large class (every row takes the one-thread or one-warp path,
+// whose exact count costs about what the prediction does) has nothing for the
+// prediction to skip, so the plain path finishes it on the same tiles and
+// bounds.  Either way the output is the plain path's, bit for bit.
 int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
                         const hsmu_opts *opts, cudaStream_t st, hsmu_stats *stats) {
     if (!h || !csr_ok(A) || !csr_ok(B) || !C || !model || !model->params) return HSMU_ERR_INVALID;
@@ -552,10 +635,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     if (o.arith < HSMU_ARITH_RN || o.arith > HSMU_ARITH_IMUL) return HSMU_ERR_INVALID;
     const int M = A->M;
     int rc = HSMU_OK;
-    Ctl *ctl = nullptr;
-    hsmu_btiles bt{};
-    RowInfo ri{};
-    int *scan_tmp = nullptr, *cap = nullptr, *crp = nullptr, *ccol = nullptr, *scol = nullptr;
+    int *cap = nullptr, *crp = nullptr, *ccol = nullptr, *scol = nullptr;
     long long *soff = nullptr;
     float4 *feat = nullptr;
     unsigned char *flag = nullptr;
@@ -564,113 +644,133 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     long long win_cap = 0, spec_total = 0, cur_cap = 0;
     WinCursors wc{};
     Ctl hc{};
-    DevCSR Ad = dev(A), Bd = dev(B);
-    DevTiles Btd{};
     std::memset(C, 0, sizeof(*C));
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         cudaEventRecord(h->ev[0], st);
     }
-    CK(palloc(&ctl, 1, st));
-    CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
-    if (o.validate) {
-        launch_validate(Ad, ctl, grid_rows(h), st);
-        launch_validate(Bd, ctl, grid_rows(h), st);
+    PlainRun r(h, st, o);
+    rc = r.begin(A, B);
+    if (!rc) rc = r.tiles_bounds(B, nullptr, stats != nullptr, stats ? h->ev[1] : nullptr, false);
+    if (rc) goto done;
+    CK(cudaMemcpyAsync(h->h_ctl, r.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    hc = *h->h_ctl;
+    if (hc.err) {
+        rc = err_from_dev(hc.err);
+        goto done;
+    }
+    if (hc.bin_count[BIN_L] == 0) {
+        // the plain path on the same tiles and bounds
+        rc = r.count_scan(nullptr);
+        if (!rc && stats) cudaEventRecord(h->ev[2], st);
+        if (!rc) rc = r.alloc_output();
+        if (!rc) {
+            if (stats) cudaEventRecord(h->ev[3], st);
+            r.structure(0, M);
+            if (stats) cudaEventRecord(h->ev[4], st);
+            r.values();
+            if (stats) cudaEventRecord(h->ev[5], st);
+            rc = r.finish();
+        }
+        if (rc) goto done;
+        C->M = M;
+        C->N = B->N;
+        C->nnz = (int32_t)r.hc.nnz;
+        C->owned = 1;
+        C->row_ptr = r.crp;
+        C->col = r.ccol;
+        C->val = r.cval;
+        r.crp = nullptr;
+        r.ccol = nullptr;
+        r.cval = nullptr;
+        if (stats) {
+            fill_stats(h, r, nullptr, stats);
+            stats->routed = 1;
+        }
+        goto done;
+    }
+    {
+        Ctl *ctl = r.ctl;
+        const DevCSR &Ad = r.Ad, &Bd = r.Bd;
+        const DevTiles &Btd = r.Btd;
+        RowInfo &ri = r.ri;
+        CK(palloc(&feat, (size_t)M, st));
+        CK(palloc(&cap, (size_t)M + 1, st));
+        CK(palloc(&soff, (size_t)M + 1, st));
+        CK(palloc(&flag, (size_t)M, st));
+        CK(cudaMemsetAsync(flag, 0, (size_t)M, st));
+        launch_features(Ad, Bd, feat, nullptr, h->nsm, st);
+        launch_capacity(model->params, feat, ri.prod, M, B->N, model->margin, cap, h->nsm, st);
+        launch_scan64(cap, soff, M, &ctl->nnz, r.scan_tmp, st);  // nnz field holds the slot total for now
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if (h->h_ctl->err) {
-            rc = err_from_dev(h->h_ctl->err);
+        hc = *h->h_ctl;
+        if (stats) cudaEventRecord(h->ev[2], st);
+        if (hc.err) {
+            rc = err_from_dev(hc.err);
             goto done;
         }
-    }
-    rc = build_tiles(h, B, &bt, ctl, 0, st, stats != nullptr);
-    if (rc) goto done;
-    Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
-    if (stats) cudaEventRecord(h->ev[1], st);
-    CK(palloc(&ri.prod, (size_t)M, st));
-    CK(palloc(&ri.tmin, (size_t)M, st));
-    CK(palloc(&ri.tmax, (size_t)M, st));
-    CK(palloc(&ri.bins, (size_t)M * NBIN, st));
-    CK(palloc(&ri.cls, (size_t)M, st));
-    CK(palloc(&ri.bin_cnt, bin_scratch_ints(M), st));
-    CK(palloc(&ri.cnnz, (size_t)M + 1, st));
-    CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
-    CK(palloc(&feat, (size_t)M, st));
-    CK(palloc(&cap, (size_t)M + 1, st));
-    CK(palloc(&soff, (size_t)M + 1, st));
-    CK(palloc(&flag, (size_t)M, st));
-    CK(cudaMemsetAsync(flag, 0, (size_t)M, st));
-    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
-    launch_features(Ad, Bd, feat, nullptr, h->nsm, st);
-    launch_capacity(model->params, feat, ri.prod, M, B->N, model->margin, cap, h->nsm, st);
-    launch_scan64(cap, soff, M, &ctl->nnz, scan_tmp, st);  // nnz field holds the slot total for now
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    hc = *h->h_ctl;
-    if (stats) cudaEventRecord(h->ev[2], st);
-    if (hc.err) {
-        rc = err_from_dev(hc.err);
-        goto done;
-    }
-    spec_total = hc.nnz;
-    win_cap = 2 * (long long)hc.win_bound;  // speculative pass + redo of overflowing rows
-    if (win_cap > INT_MAX) {
-        rc = HSMU_ERR_OVERFLOW;
-        goto done;
-    }
-    CK(palloc(&scol, (size_t)spec_total + COL_PAD, st));
-    CK(palloc(&sval, (size_t)spec_total, st));
-    CK(palloc(&win, (size_t)win_cap, st));
-    CK(palloc(&crp, (size_t)M + 1, st));
-    // cursors of the windows of both passes (no exact count pass: every warp row above FUSE_CAP products)
-    cur_cap = 2 * (long long)(hc.cur_bound + hc.cur_bound_ds);
-    if (win_cap > 0) {
-        wc.cap = cur_cap;
-        CK(palloc(&wc.len, (size_t)win_cap, st));
-        CK(palloc(&wc.off, (size_t)win_cap + 1, st));
-        CK(palloc(&wc.total, 1, st));
-        CK(palloc(&wc.scan_tmp, scan_tmp_ints((int)win_cap), st));
-        CK(palloc(&wc.cur, (size_t)cur_cap, st));
-    }
-    if (stats) cudaEventRecord(h->ev[3], st);
-    // structure (+ values of warp-sized rows) into the slots; exact counts found here
-    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M}, win, win_cap, ctl,
-                     o.arith, h->nsm, st);
-    launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
-    // exact nnz(C): rows that overflowed their slot can make it larger than the slot total
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    hc = *h->h_ctl;
-    if (hc.err) {
-        rc = err_from_dev(hc.err);
-        goto done;
-    }
-    if (hc.nnz > INT_MAX) {
-        rc = HSMU_ERR_OVERFLOW;
-        goto done;
-    }
-    CK(palloc(&ccol, (size_t)hc.nnz + COL_PAD, st));
-    CK(palloc(&cval, (size_t)hc.nnz, st));
-    launch_compact(M, soff, crp, flag, scol, sval, ccol, cval, h->nsm, st);
-    launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag, 0, M}, win, win_cap, ctl,
-                     o.arith, h->nsm, st);
-    if (stats) cudaEventRecord(h->ev[4], st);
-    launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, flag, scol, soff, wc, ctl, o.arith, h->nsm, st);
-    CK(cudaGetLastError());
-    if (stats) cudaEventRecord(h->ev[5], st);
-    CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    hc = *h->h_ctl;
-    if (hc.err) {
-        rc = err_from_dev(hc.err);
-        goto done;
-    }
-    if (hc.nnz > INT_MAX) {
-        rc = HSMU_ERR_OVERFLOW;
-        goto done;
+        spec_total = hc.nnz;
+        win_cap = 2 * (long long)hc.win_bound;  // speculative pass + redo of overflowing rows
+        if (win_cap > INT_MAX) {
+            rc = HSMU_ERR_OVERFLOW;
+            goto done;
+        }
+        CK(palloc(&scol, (size_t)spec_total + COL_PAD, st));
+        CK(palloc(&sval, (size_t)spec_total, st));
+        CK(palloc(&win, (size_t)win_cap, st));
+        CK(palloc(&crp, (size_t)M + 1, st));
+        // cursors of the windows of both passes (no exact count pass: every warp row above FUSE_CAP products)
+        cur_cap = 2 * (long long)(hc.cur_bound + hc.cur_bound_ds);
+        if (win_cap > 0) {
+            wc.cap = cur_cap;
+            CK(palloc(&wc.len, (size_t)win_cap, st));
+            CK(palloc(&wc.off, (size_t)win_cap + 1, st));
+            CK(palloc(&wc.total, 1, st));
+            CK(palloc(&wc.scan_tmp, scan_tmp_ints((int)win_cap), st));
+            CK(palloc(&wc.cur, (size_t)cur_cap, st));
+        }
+        if (stats) cudaEventRecord(h->ev[3], st);
+        // structure (+ values of warp-sized rows) into the slots; exact counts found here
+        launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M}, win,
+                         win_cap, ctl, o.arith, h->nsm, st);
+        launch_scan(ri.cnnz, crp, M, &ctl->nnz, r.scan_tmp, ctl, st);
+        // exact nnz(C): rows that overflowed their slot can make it larger than the slot total
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        hc = *h->h_ctl;
+        if (hc.err) {
+            rc = err_from_dev(hc.err);
+            goto done;
+        }
+        if (hc.nnz > INT_MAX) {
+            rc = HSMU_ERR_OVERFLOW;
+            goto done;
+        }
+        CK(palloc(&ccol, (size_t)hc.nnz + COL_PAD, st));
+        CK(palloc(&cval, (size_t)hc.nnz, st));
+        launch_compact(M, soff, crp, flag, scol, sval, ccol, cval, h->nsm, st);
+        launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag, 0, M}, win,
+                         win_cap, ctl, o.arith, h->nsm, st);
+        if (stats) cudaEventRecord(h->ev[4], st);
+        launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, flag, scol, soff, wc, ctl, o.arith, h->nsm, st,
+                       o.wait_polls);
+        CK(cudaGetLastError());
+        if (stats) cudaEventRecord(h->ev[5], st);
+        CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        hc = *h->h_ctl;
+        if (hc.err) {
+            rc = err_from_dev(hc.err);
+            goto done;
+        }
+        if (hc.nnz > INT_MAX) {
+            rc = HSMU_ERR_OVERFLOW;
+            goto done;
+        }
     }
     C->M = M;
     C->N = B->N;
@@ -707,19 +807,6 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         stats->launches = (o.validate ? 2 : 0) + (win_cap > 0 ? 32 : 27);
     }
 done:
-    pfree(ctl, st);
-    pfree(bt.tile_ptr, st);
-    pfree(bt.tile_col, st);
-    pfree(bt.mask, st);
-    pfree(bt.tile_off, st);
-    pfree(ri.prod, st);
-    pfree(ri.tmin, st);
-    pfree(ri.tmax, st);
-    pfree(ri.bins, st);
-    pfree(ri.cls, st);
-    pfree(ri.bin_cnt, st);
-    pfree(ri.cnnz, st);
-    pfree(scan_tmp, st);
     pfree(feat, st);
     pfree(cap, st);
     pfree(soff, st);
@@ -735,6 +822,7 @@ done:
     pfree(crp, st);
     pfree(ccol, st);
     pfree(cval, st);
+    r.release();
     if (rc != HSMU_OK) cudaStreamSynchronize(st);
     return rc;
 }
@@ -906,12 +994,17 @@ int hsmu_handle_create(hsmu_handle *out) {
         delete h;
         return HSMU_ERR_ALLOC;
     }
+    if (cudaMallocHost(reinterpret_cast<void **>(&h->h_mid), sizeof(Ctl)) != cudaSuccess) {
+        hsmu_handle_destroy(h);
+        return HSMU_ERR_ALLOC;
+    }
     for (auto &e : h->ev) cudaEventCreate(&e);
     if (cudaStreamCreateWithFlags(&h->cs_in, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->cs_out, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_mid, cudaEventDisableTiming) != cudaSuccess) {
         hsmu_handle_destroy(h);
         return HSMU_ERR_CUDA;
     }
@@ -936,11 +1029,12 @@ int hsmu_handle_destroy(hsmu_handle h) {
     if (!h) return HSMU_OK;
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out})
+    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out, h->ev_mid})
         if (e) cudaEventDestroy(e);
     for (cudaStream_t s : {h->cs_in, h->cs_out})
         if (s) cudaStreamDestroy(s);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
+    if (h->h_mid) cudaFreeHost(h->h_mid);
     delete h;
     return HSMU_OK;
 }
@@ -1097,6 +1191,21 @@ int hsmu_selftest_dmul(uint64_t n, uint64_t seed, uint64_t *mismatches, void *st
     int e = run_dmul_selftest(n, seed, &m, static_cast<cudaStream_t>(stream));
     *mismatches = m;
     return e ? HSMU_ERR_CUDA : HSMU_OK;
+}
+
+int hsmu_debug_fail_alloc(int64_t nth) {
+    if (nth < 0) return HSMU_ERR_INVALID;
+    g_fail_alloc_countdown.store((long long)nth, std::memory_order_relaxed);
+    return HSMU_OK;
+}
+
+int hsmu_probe_fp64_rate(int iters, double *lane_ops_per_s, void *stream) {
+    if (!lane_ops_per_s || iters <= 0) return HSMU_ERR_INVALID;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return HSMU_ERR_NO_DEVICE;
+    return run_fp64_rate(iters, nsm, lane_ops_per_s, static_cast<cudaStream_t>(stream)) ? HSMU_ERR_CUDA : HSMU_OK;
 }
 
 int hsmu_csr_download(const hsmu_csr *C, int32_t *row_ptr, int32_t *col, double *val, void *stream) {

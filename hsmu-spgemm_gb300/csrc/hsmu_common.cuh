@@ -82,6 +82,7 @@ struct Ctl {
                                      // rows (bounds pass) + warp rows above FUSE_CAP (count pass)
     unsigned long long cur_bound_ds; // same for every warp row with more than FUSE_CAP products
                                      // (bounds pass; for paths without a count pass)
+    long long store_tiles;           // sum of RowInfo::tcap (entries of the tile store)
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -203,6 +204,21 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
         unsigned done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// at most `polls` non-blocking tests of the barrier's phase `parity`
+// (mbarrier.test_wait never suspends the thread); false if it has not completed
+__device__ __forceinline__ bool mbar_poll(unsigned long long *bar, unsigned parity, int polls) {
+    for (int it = 0; it < polls; it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
             : "r"(smem_u32(bar)), "r"(parity)
             : "memory");

@@ -48,6 +48,19 @@ struct RowInfo {
     signed char *cls;  // row class (RowBin) of every row, -1 for an empty row
     int *bin_cnt;      // [NBIN][ceil(M/32)] rows of each class per 32-row chunk, then
                        // its exclusive scan (bin_scratch_ints(M) entries)
+    int *tcap;         // nullable: C tiles a large-class row can have, min(tile span, sum of
+                       // its B rows' tile counts); 0 for the other rows (bounds pass)
+};
+
+// C tiles of the large-class rows, kept by the count pass (which builds them
+// anyway) so that the structure pass streams each row's tile list instead of
+// repeating the OR walk over B's tiles.  Row i's list: tcol/tmask[off[i] ..
+// off[i] + cnt[i]), tile ids ascending; off is the scan of RowInfo::tcap.
+struct TileStore {
+    const long long *off;       // [M+1]
+    int *cnt;                   // [M] tiles stored per row
+    int *tcol;                  // tile ids
+    unsigned long long *tmask;  // column masks
 };
 
 // scratch ints of RowInfo::bin_cnt for M rows
@@ -64,6 +77,7 @@ void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo
                    cudaStream_t st);
 // exclusive scan of int counts (n entries) into out[0..n]; total (int64) into *total64;
 // sets DERR_OVERFLOW if the total exceeds INT32_MAX.  tmp must hold scan_tmp_ints(n) ints.
+// in == out (an in-place scan) is allowed.
 size_t scan_tmp_ints(int n);
 void launch_scan(const int *in, int *out, int n, long long *total64, int *tmp, Ctl *ctl, cudaStream_t st);
 // same with int64 output (no overflow limit)
@@ -79,13 +93,20 @@ void launch_compact(int M, const long long *soff, const int *crp, const unsigned
 // k_symbolic.cu
 void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
                   cudaStream_t st);
+// the same in two launches: rows of the tiny and warp classes, then the large class
+// (ts: nullable; when given, every large row's C tiles are stored)
+void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
+                        cudaStream_t st);
+void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,
+                        cudaStream_t st);
 
 // k_structure.cu
 // writes C's columns and numeric windows; rows that fit one warp also get their values
 // class_rows: rows per class (BIN_*) when known on the host; kernels of empty classes are skipped
+// ts (nullable, PLAIN mode): large rows are built from their stored tile lists
 void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
                       long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st,
-                      const int *class_rows = nullptr);
+                      const int *class_rows = nullptr, const TileStore *ts = nullptr);
 
 // k_numeric.cu
 // flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped;
@@ -103,9 +124,15 @@ struct WinCursors {
 };
 void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
-                    const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st);
+                    const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st,
+                    int wait_polls = 0);
 
 int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st);
+// FP64 lane operations per second of a full-grid chain probe
+int run_fp64_rate(int iters, int nsm, double *lane_ops_per_s, cudaStream_t st);
+
+// hsmu_status of the device error bits collected in Ctl::err (0 -> HSMU_OK)
+int status_from_dev_err(int err);
 
 // smem sizes are set once per device (cudaFuncSetAttribute)
 int configure_kernels();

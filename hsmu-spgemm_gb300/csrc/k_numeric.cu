@@ -120,7 +120,8 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             const int *__restrict__ scol,
                                                             const long long *__restrict__ soff,
                                                             const long long *__restrict__ woff,
-                                                            const int *__restrict__ wcur, Ctl *ctl) {
+                                                            const int *__restrict__ wcur, int wait_polls,
+                                                            Ctl *ctl) {
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
@@ -161,10 +162,16 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             if (lane == 0) bulk_g2s(stage, reinterpret_cast<const void *>(ga & ~(uintptr_t)15), bytes, &S.bar);
             for (int q = lane; q < WIN_TCAP; q += WARP) S.tmask[q] = 0ull;
             for (int q = lane; q < WIN_OCCW; q += WARP) S.occ[q] = 0ull;
-            const bool arrived = mbar_wait(&S.bar, phase, STAGE_LIMIT) || mbar_wait(&S.bar, phase, STAGE_LIMIT);
+            // wait_polls > 0 (a test hook): that many non-blocking polls, then give up
+            const bool arrived = wait_polls > 0 ? mbar_poll(&S.bar, phase, wait_polls)
+                                                : mbar_wait(&S.bar, phase, STAGE_LIMIT) ||
+                                                      mbar_wait(&S.bar, phase, STAGE_LIMIT);
             if (!__all_sync(FULL, arrived)) {
                 if (lane == 0) set_err(&ctl->err, DERR_TIMEOUT);
-                return;  // the copy never completed: leave the kernel
+                // the copy still targets this warp's shared memory: let it land (bounded)
+                // before the warp leaves the kernel
+                mbar_wait(&S.bar, phase, STAGE_LIMIT) || mbar_wait(&S.bar, phase, STAGE_LIMIT);
+                return;
             }
             phase ^= 1u;
             const int *src = stage + lead;
@@ -307,7 +314,8 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
 
 void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
-                    const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st) {
+                    const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st,
+                    int wait_polls) {
     if (win_cap <= 0) return;
     cudaMemsetAsync(&ctl->win_next, 0, sizeof(int), st);
     k_win_len<<<nsm * 4, 256, 0, st>>>(win, (int)win_cap, A.rp, ctl, wc.len);
@@ -317,7 +325,7 @@ void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const 
     auto k = arith == AR_IMUL ? k_numeric<AR_IMUL> : arith == AR_FMA ? k_numeric<AR_FMA> : k_numeric<AR_RN>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
         A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, wc.off, wc.cur,
-        ctl);
+        wait_polls, ctl);
 }
 
 int configure_numeric() {
@@ -366,6 +374,54 @@ __global__ void k_dmul_selftest(unsigned long long n, unsigned long long seed, u
         if (!nan2 && dbits(x) != dbits(y)) bad++;
     }
     if (bad) atomicAdd(mism, bad);
+}
+
+// FP64 pipe throughput probe: 8 multiply chains and 8 add chains per thread,
+// independent of each other (no FMA: __dmul_rn / __dadd_rn keep them apart)
+__global__ void __launch_bounds__(256) k_fp64_rate(int iters, double seed, double *out) {
+    double m[8], a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        m[j] = seed + 1e-3 * (threadIdx.x + j);
+        a[j] = seed - 1e-3 * (threadIdx.x + j);
+    }
+    const double f = 1.0 + 1e-12, d = 1e-15;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            m[j] = __dmul_rn(m[j], f);
+            a[j] = __dadd_rn(a[j], d);
+        }
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += m[j] + a[j];
+    if (s == 12345.678) out[threadIdx.x] = s;  // keeps the chains alive; never true for these inputs
+}
+
+int run_fp64_rate(int iters, int nsm, double *lane_ops_per_s, cudaStream_t st) {
+    const int blocks = nsm * 8, threads = 256;
+    double *d = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMallocAsync(&d, threads * sizeof(double), st);
+    if (!e) e = cudaEventCreate(&e0);
+    if (!e) e = cudaEventCreate(&e1);
+    if (!e) {
+        k_fp64_rate<<<blocks, threads, 0, st>>>(iters / 8 + 1, 1.0, d);  // warm-up
+        cudaEventRecord(e0, st);
+        k_fp64_rate<<<blocks, threads, 0, st>>>(iters, 1.0, d);
+        cudaEventRecord(e1, st);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (!e) *lane_ops_per_s = (double)blocks * threads * (double)iters * 16.0 / (ms * 1e-3);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (d) cudaFreeAsync(d, st);
+    cudaStreamSynchronize(st);
+    return (int)e;
 }
 
 int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st) {

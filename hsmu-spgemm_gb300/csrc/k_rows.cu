@@ -37,13 +37,14 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     __syncthreads();
     for (int rb = blockIdx.x * RPB; rb < M; rb += gridDim.x * RPB) {
         const int i = rb + rloc;
-        long long prod = 0;
+        long long prod = 0, tsum = 0;
         int tmin = INT_MAX, tmax = -1;
         if (i < M) {
             for (int p = arp[i] + sub; p < arp[i + 1]; p += G) {
                 const int k = __ldg(acol + p);
                 prod += __ldg(brp + k + 1) - __ldg(brp + k);
                 const int t0 = __ldg(tptr + k), t1 = __ldg(tptr + k + 1);
+                tsum += t1 - t0;
                 if (t1 > t0) {
                     tmin = min(tmin, __ldg(tcol + t0));
                     tmax = max(tmax, __ldg(tcol + t1 - 1));
@@ -53,6 +54,7 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
 #pragma unroll
         for (int d = G / 2; d > 0; d >>= 1) {
             prod += __shfl_xor_sync(FULL, prod, d, G);
+            tsum += __shfl_xor_sync(FULL, tsum, d, G);
             tmin = min(tmin, __shfl_xor_sync(FULL, tmin, d, G));
             tmax = max(tmax, __shfl_xor_sync(FULL, tmax, d, G));
         }
@@ -78,6 +80,11 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                 if (bin == BIN_DS && prod > FUSE_CAP) my_cbd += wb * (unsigned long long)(arp[i + 1] - arp[i]);
             }
             ri.cls[i] = (signed char)bin;
+            if (ri.tcap) {
+                // a large row has at most one C tile per tile of its span and per B tile it reads
+                const long long span = prod ? (long long)(tmax - tmin + 1) : 0;
+                ri.tcap[i] = bin == BIN_L ? (int)(tsum < span ? tsum : span) : 0;
+            }
         }
     }
     __syncthreads();
@@ -195,7 +202,11 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_top(long long *bsum, int nb, lo
     if (threadIdx.x == 0) *total64 = carry;
 }
 
-__global__ void __launch_bounds__(SCAN_T) k_scan_out(const int *__restrict__ in, int *__restrict__ out, int n,
+// in and out may be the same array (in-place scan; the allocation-free tile conversion and the
+// AMG generators rely on it), so neither is __restrict__: every thread loads its SCAN_IPT items
+// into registers before the block scan's barriers and afterwards stores only those same items,
+// blocks cover disjoint ranges, and out[n] lies past every item read.
+__global__ void __launch_bounds__(SCAN_T) k_scan_out(const int *in, int *out, int n,
                                                      const long long *__restrict__ boff, const long long *total64,
                                                      Ctl *ctl) {
     __shared__ long long s_warp[SCAN_T / 32 + 1];

@@ -393,6 +393,116 @@ __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__
     }
 }
 
+// ---- large rows from their stored C tiles (PLAIN mode, tile store present)
+// The count pass kept every large row's non-empty C tiles (ascending ids and
+// masks), so the row needs no second OR walk over B: the CTA streams the list
+// NT tiles at a time -- slot of each tile (block scan of popcounts), window key
+// (block max-scan), window starts (block scan) -- twice: the first pass counts
+// the row's windows so that one atomic reserves them contiguously (the value
+// pass relies on a row's windows being neighbours), the second writes the
+// windows and the columns (lane per tile, lowest bit first).  Windows are cut
+// where the tile's first slot crosses a multiple of WIN_CUT, its rank crosses a
+// multiple of WIN_TCAP, or its offset from the row's first tile crosses a
+// multiple of WIN_SPAN -- the limits of k_numeric's tables.
+constexpr int SLS_THREADS = 256;
+
+__device__ __forceinline__ long long win_key_row(int slot, int rank, int toff) {
+    return ((long long)(slot / WIN_CUT) << 40) | ((long long)(rank / WIN_TCAP) << 20) | (long long)(toff / WIN_SPAN);
+}
+
+__global__ void __launch_bounds__(SLS_THREADS) k_struct_ls(int M, RowInfo ri, TileStore ts, RowOut out,
+                                                           Window *__restrict__ win, long long win_cap, Ctl *ctl) {
+    constexpr int NT = SLS_THREADS;
+    __shared__ int s_slot[NT / 32], s_st[NT / 32];
+    __shared__ long long s_key[NT / 32];
+    __shared__ int s_wbase;
+    const int *rows = ri.bins + (size_t)BIN_L * M;
+    int b0, b1;
+    bin_slice(rows, ctl->bin_count[BIN_L], out, M, b0, b1);
+    int *__restrict__ ccol = out.ccol;
+    for (int r = b0 + blockIdx.x; r < b1; r += gridDim.x) {
+        const int i = rows[r];
+        if (skip_row(out, i)) continue;
+        const int n = ts.cnt[i];
+        const long long sb = ts.off[i];
+        const int tmin = ri.tmin[i];
+        const long long rowbase = out.crp[i];
+        const int nnz = out.crp[i + 1] - out.crp[i];
+        int wbase = 0, nwin = 0;
+        for (int pass = 0; pass < 2; pass++) {
+            int run = 0, wrun = 0;
+            long long carry = -1;
+            for (int blk = 0; blk < n; blk += NT) {
+                const int q = blk + (int)threadIdx.x;
+                const bool v = q < n;
+                const int t = v ? __ldg(ts.tcol + sb + q) : 0;
+                const unsigned long long m = v ? __ldg(ts.tmask + sb + q) : 0ull;
+                int btot;
+                const int slot = block_excl_sum1<NT>(popc64(m), s_slot, btot) + run;
+                const long long key = v ? win_key_row(slot, q, t - tmin) : -1ll;
+                long long kmax;
+                const long long prev = block_excl_max1t<NT>(key, s_key, carry, kmax);
+                const bool start = v && key != prev;
+                int nst;
+                const int wpos = block_excl_sum1<NT>((int)start, s_st, nst) + wrun;
+                if (pass == 1) {
+                    if (start) {
+                        if (wpos < nwin) win[wbase + wpos] = Window{i, slot, 0, t, 0};
+                        else set_err(&ctl->err, DERR_INTERNAL);
+                    }
+                    // this thread's tile: lanes of a warp write their tiles' columns together
+                    // (every lane takes part in the step count; a tile past the row's end is
+                    // an internal error and writes nothing)
+                    const bool fits = slot + popc64(m) <= nnz;
+                    if (!fits) set_err(&ctl->err, DERR_INTERNAL);
+                    unsigned long long mm = fits ? m : 0ull;
+                    int *o = ccol + rowbase + slot;
+                    const int cb = t << 6;
+                    const int steps = (int)__reduce_max_sync(FULL, (unsigned)popc64(mm));
+                    for (int k = 0; k < steps; k++) {
+                        if (mm) {
+                            *o++ = cb + (__ffsll((long long)mm) - 1);
+                            mm &= mm - 1ull;
+                        }
+                    }
+                }
+                run += btot;
+                wrun += nst;
+                carry = kmax;
+            }
+            if (pass == 0) {
+                if (threadIdx.x == 0) {
+                    int wb = -1;
+                    if (run != nnz) {
+                        set_err(&ctl->err, DERR_INTERNAL);
+                    } else if (wrun > 0) {
+                        wb = atomicAdd(&ctl->win_count, wrun);
+                        if ((long long)wb + wrun > win_cap) {
+                            set_err(&ctl->err, DERR_CAPACITY);
+                            wb = -1;
+                        }
+                    }
+                    s_wbase = wb;
+                }
+                __syncthreads();
+                wbase = s_wbase;
+                nwin = wrun;
+                if (wbase < 0) break;  // no windows, or an error already reported
+            }
+        }
+        __syncthreads();  // the row's window starts, written by this block, are visible to it
+        if (wbase >= 0) {
+            // every window's slot count: the next window's first slot, or the row's end
+            for (int j = threadIdx.x; j < nwin; j += NT) {
+                const int s0 = win[wbase + j].s0;
+                const int e = j + 1 < nwin ? win[wbase + j + 1].s0 : nnz;
+                win[wbase + j].cnt = e - s0;
+            }
+        }
+        __syncthreads();  // s_wbase and the scan arrays are reused by the next row
+    }
+}
+
 constexpr int TINYF_THREADS = 128;
 
 // tiny rows: one thread per row writes its sorted columns and values
@@ -429,7 +539,8 @@ __global__ void __launch_bounds__(TINYF_THREADS) k_fill_tiny(int M, const int *_
 }
 
 void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, RowOut out, Window *win,
-                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st, const int *class_rows) {
+                      long long win_cap, Ctl *ctl, int arith, int nsm, cudaStream_t st, const int *class_rows,
+                      const TileStore *ts) {
     if (!class_rows || class_rows[BIN_TINY] > 0) {
         auto kt = arith == AR_IMUL ? k_fill_tiny<AR_IMUL> : arith == AR_FMA ? k_fill_tiny<AR_FMA> : k_fill_tiny<AR_RN>;
         kt<<<nsm * 4, TINYF_THREADS, 0, st>>>(A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, ri, out, ctl);
@@ -439,9 +550,13 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
         kds<<<nsm * SDS_CTAS_PER_SM, SDS_WARPS * 32, SDS_WARPS * sizeof(SdsSmem), st>>>(
             A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
     }
-    if (!class_rows || class_rows[BIN_L] > 0)
-        k_struct_l<<<nsm * 3, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
-                                                                win, win_cap, ctl);
+    if (!class_rows || class_rows[BIN_L] > 0) {
+        if (ts && ts->tcol && out.mode == OUT_PLAIN)
+            k_struct_ls<<<nsm * 8, SLS_THREADS, 0, st>>>(A.M, ri, *ts, out, win, win_cap, ctl);
+        else
+            k_struct_l<<<nsm * 3, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
+                                                                    win, win_cap, ctl);
+    }
 }
 
 int configure_structure() {

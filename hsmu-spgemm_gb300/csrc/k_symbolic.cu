@@ -14,6 +14,11 @@
 //                search when the span needs more than one chunk.
 // Every B tile access is a coalesced 4+8 byte load of the flat (A entry,
 // B tile) sequence, 32 lanes busy regardless of row lengths.
+// With a tile store, the large-row pass also writes every row's non-empty C
+// tiles (id + mask, ascending) to the store, compacted chunk by chunk with one
+// block scan, so that the structure pass can stream them (the reference
+// likewise keeps C's tiles between its symbolic passes, C->d_tile_col /
+// C->d_mask_num, src/compressed/compressed_tileOR.cuh:389-623).
 #include "hsmu_block.cuh"
 #include "hsmu_kernels.h"
 #include "hsmu_rowops.cuh"
@@ -59,16 +64,19 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
 }
 
 constexpr int L_THREADS = 256;
+constexpr int L_PER = DCH_COUNT / L_THREADS;  // consecutive tiles per thread when storing
 
+template <bool STORE>
 __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restrict__ arp,
                                                        const int *__restrict__ acol,
                                                        const int *__restrict__ tptr,
                                                        const int *__restrict__ tcol,
                                                        const unsigned long long *__restrict__ tmask,
-                                                       RowInfo ri, Ctl *ctl) {
+                                                       RowInfo ri, TileStore ts, Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     unsigned long long *msk = s_dyn;  // DCH_COUNT entries
     __shared__ int s_red[L_THREADS / 32];
+    __shared__ long long s_pk[L_THREADS / 32];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     constexpr int NWARP = L_THREADS / 32;
     const int n = ctl->bin_count[BIN_L];
@@ -78,7 +86,9 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
         const int a_lo = arp[i], a_hi = arp[i + 1];
         const bool one_chunk = (tmax - tmin + 1) <= DCH_COUNT;
-        int total = 0;
+        int total = 0, stored = 0;
+        const long long sbase = STORE ? ts.off[i] : 0;
+        const int scap = STORE ? ri.tcap[i] : 0;
         for (int c0 = tmin; c0 <= tmax; c0 += DCH_COUNT) {
             const int c1 = min(c0 + DCH_COUNT, tmax + 1);
             for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) msk[t] = 0ull;
@@ -90,19 +100,53 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
                 warp_or_tiles<true, true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
-            int cnt = 0;
-            for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) cnt += popc64(msk[t]);
-            cnt = warp_sum(cnt);
-            if (lane == 0) s_red[w] = cnt;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                int s = 0;
-                for (int j = 0; j < NWARP; j++) s += s_red[j];
-                total += s;
+            if (STORE) {
+                // each thread: L_PER consecutive tiles; one packed block scan gives the
+                // chunk's entries and every thread's place in the row's tile list
+                const int len = c1 - c0;
+                const int lo = min(len, (int)threadIdx.x * L_PER), hi = min(len, lo + L_PER);
+                int pc = 0, ne = 0;
+                for (int t = lo; t < hi; t++) {
+                    const unsigned long long m = msk[t];
+                    pc += popc64(m);
+                    ne += m != 0ull;
+                }
+                long long tot;
+                const long long ex = block_excl_sum1<L_THREADS>(((long long)pc << 32) | ne, s_pk, tot);
+                const int chunk_tiles = (int)(tot & 0xffffffffll);
+                if (stored + chunk_tiles > scap) {
+                    if (threadIdx.x == 0) set_err(&ctl->err, DERR_INTERNAL);
+                } else {
+                    long long pos = sbase + stored + (int)(ex & 0xffffffffll);
+                    for (int t = lo; t < hi; t++) {
+                        const unsigned long long m = msk[t];
+                        if (m) {
+                            ts.tcol[pos] = c0 + t;
+                            ts.tmask[pos] = m;
+                            pos++;
+                        }
+                    }
+                }
+                stored += chunk_tiles;
+                total += (int)(tot >> 32);
+            } else {
+                int cnt = 0;
+                for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) cnt += popc64(msk[t]);
+                cnt = warp_sum(cnt);
+                if (lane == 0) s_red[w] = cnt;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    int s = 0;
+                    for (int j = 0; j < NWARP; j++) s += s_red[j];
+                    total += s;
+                }
             }
             __syncthreads();
         }
-        if (threadIdx.x == 0) ri.cnnz[i] = total;
+        if (threadIdx.x == 0) {
+            ri.cnnz[i] = total;
+            if (STORE) ts.cnt[i] = min(stored, scap);  // over the capacity: reported above
+        }
     }
 }
 
@@ -126,17 +170,35 @@ __global__ void __launch_bounds__(TINY_THREADS) k_count_tiny(int M, const int *_
     if (bad) set_err(&ctl->err, DERR_INTERNAL);
 }
 
-void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
-                  cudaStream_t st) {
+void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
+                        cudaStream_t st) {
     k_count_tiny<<<nsm * 4, TINY_THREADS, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, ri, ctl);
     k_count_ds<<<nsm * 6, DS_WARPS * 32, 0, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, ctl);
-    k_count_l<<<nsm * 6, L_THREADS, DCH_COUNT * sizeof(unsigned long long), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col,
-                                                                                   Bt.mask, ri, ctl);
+}
+
+void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,
+                        cudaStream_t st) {
+    const size_t smem = DCH_COUNT * sizeof(unsigned long long);
+    if (ts && ts->tcol && ri.tcap)
+        k_count_l<true><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, *ts, ctl);
+    else
+        k_count_l<false><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri,
+                                                           TileStore{}, ctl);
+}
+
+void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
+                  cudaStream_t st) {
+    launch_count_small(A, B, Bt, ri, ctl, nsm, st);
+    launch_count_large(A, Bt, ri, nullptr, ctl, nsm, st);
 }
 
 int configure_count() {
-    return (int)cudaFuncSetAttribute(k_count_l, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     DCH_COUNT * (int)sizeof(unsigned long long));
+    for (auto k : {k_count_l<false>, k_count_l<true>}) {
+        const int e = (int)cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                DCH_COUNT * (int)sizeof(unsigned long long));
+        if (e) return e;
+    }
+    return 0;
 }
 
 }  // namespace hsmu

@@ -19,7 +19,10 @@
 // Set-up: the device address of the array is looked up with
 // cudaGetSymbolAddress once per device, by the first call made while that
 // device is current (so make the first call on each device before any
-// stream capture).  All calls share the array and it keeps the previous
+// stream capture).  The address is cached for the life of the process:
+// cudaDeviceReset (or any reset of the device's primary context) reloads
+// the module and invalidates it, so do not call this entry point again on a
+// device after resetting it.  All calls share the array and it keeps the previous
 // call's contents: each call clears the control word itself, and calls that
 // overlap on the GPU (different streams, or different host threads on the
 // same device) race on it -- serialise them.
@@ -82,16 +85,23 @@ extern "C" int hsmu_btiles_build_noalloc(const hsmu_csr *B, int32_t *tile_ptr, i
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return HSMU_ERR_CUDA;
     const DevCSR Bd{B->M, B->N, (long long)B->nnz, B->row_ptr, B->col, B->val};
+    // the control word keeps the previous call's bits: clear it first
     if (cudaMemsetAsync(ctl, 0, sizeof(Ctl), st) != cudaSuccess) return HSMU_ERR_CUDA;
-    // counts into tile_ptr[0..M), in-place exclusive scan (tile_ptr[M] = total), then the fill
-    launch_tiles_count(Bd, tile_ptr, 1, ctl, nsm * 8, st);
-    launch_scan(tile_ptr, tile_ptr, B->M, total, scan_tmp, ctl, st);
-    launch_tiles_fill(Bd, tile_ptr, tile_col, reinterpret_cast<unsigned long long *>(mask), tile_off, ctl, nsm * 8, st);
+    // B is checked (row pointers non-decreasing within [0, nnz], columns sorted, unique and
+    // in range) before any tile kernel indexes through it: a bad row pointer would make the
+    // fill pass write past the caller's nnz-sized tile arrays
+    launch_validate(Bd, ctl, nsm * 8, st);
     if (cudaGetLastError() != cudaSuccess) return HSMU_ERR_CUDA;
     int err = 0;
     if (cudaMemcpyAsync(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return HSMU_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return HSMU_ERR_CUDA;
-    if (err & DERR_UNSORTED) return HSMU_ERR_UNSORTED;
-    if (err) return HSMU_ERR_INTERNAL;
-    return HSMU_OK;
+    if (err) return status_from_dev_err(err);
+    // counts into tile_ptr[0..M), in-place exclusive scan (tile_ptr[M] = total), then the fill
+    launch_tiles_count(Bd, tile_ptr, 0, ctl, nsm * 8, st);
+    launch_scan(tile_ptr, tile_ptr, B->M, total, scan_tmp, ctl, st);
+    launch_tiles_fill(Bd, tile_ptr, tile_col, reinterpret_cast<unsigned long long *>(mask), tile_off, ctl, nsm * 8, st);
+    if (cudaGetLastError() != cudaSuccess) return HSMU_ERR_CUDA;
+    if (cudaMemcpyAsync(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return HSMU_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return HSMU_ERR_CUDA;
+    return status_from_dev_err(err);
 }

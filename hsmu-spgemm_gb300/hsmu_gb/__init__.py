@@ -43,7 +43,7 @@ EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_hand
            "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
            "hsmu_gen_poisson7", "hsmu_gen_aggregation", "hsmu_spgemm_learned", "hsmu_row_features",
            "hsmu_row_nnz", "hsmu_mlp_forward", "hsmu_mlp_grad", "hsmu_mlp_adam", "hsmu_spgemm64",
-           "hsmu_csr64_free", "hsmu_csr64_download"]
+           "hsmu_csr64_free", "hsmu_csr64_download", "hsmu_probe_fp64_rate", "hsmu_debug_fail_alloc"]
 MLP_FLOATS = 1259
 
 
@@ -74,7 +74,8 @@ class c_btiles(ctypes.Structure):
 
 class c_opts(ctypes.Structure):
     _fields_ = [("validate", ctypes.c_int32), ("arith", ctypes.c_int32),
-                ("window_cap", ctypes.c_int32), ("panels", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+                ("window_cap", ctypes.c_int32), ("panels", ctypes.c_int32), ("wait_polls", ctypes.c_int32),
+                ("no_tile_store", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class c_mlp(ctypes.Structure):
@@ -87,7 +88,7 @@ class c_stats(ctypes.Structure):
                 ("ms_convert", ctypes.c_float), ("ms_symbolic", ctypes.c_float),
                 ("ms_alloc", ctypes.c_float), ("ms_structure", ctypes.c_float),
                 ("ms_numeric", ctypes.c_float), ("ms_total", ctypes.c_float),
-                ("launches", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("launches", ctypes.c_int32), ("routed", ctypes.c_int32),
                 ("spec_capacity", ctypes.c_int64), ("fallback_rows", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
@@ -146,6 +147,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_mlp_grad.argtypes = [P, P, P, ctypes.c_int, P, P, P]
     L.hsmu_mlp_adam.argtypes = [P, P, P, P, ctypes.c_float, ctypes.c_float, ctypes.c_int, P]
     L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
+    L.hsmu_probe_fp64_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), P]
+    L.hsmu_debug_fail_alloc.argtypes = [ctypes.c_int64]
     L.hsmu_spgemm64.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr64),
                                 ctypes.c_int64, ctypes.POINTER(c_opts), P]
     L.hsmu_csr64_free.argtypes = [ctypes.POINTER(c_csr64)]
@@ -215,6 +218,19 @@ class DeviceCSR:
                                    val.ctypes.data, _stream_ptr(stream)), "hsmu_csr_download")
         return CSR(self.M, self.N, rp, col, val)
 
+    def row_ptr_host(self) -> np.ndarray:
+        """C's row pointers (int32[M+1]) copied to the host."""
+        rp = np.empty(self.M + 1, dtype=np.int32)
+        _memcpy_d2h(rp.ctypes.data, self.desc.row_ptr, rp.nbytes)
+        return rp
+
+    def rows_to_host(self, rows, row_ptr=None):
+        """Only the listed rows, copied to the host: (local row_ptr int64[k+1],
+        col, val) in the order of `rows`.  Runs of consecutive rows are copied
+        as one slice each, so a sample of a huge product costs a few copies."""
+        rp = self.row_ptr_host() if row_ptr is None else row_ptr
+        return _rows_from_device(rp, self.desc.col, self.desc.val, rows)
+
     def free(self):
         if self.desc.owned:
             load_library().hsmu_csr_free(ctypes.byref(self.desc))
@@ -281,6 +297,29 @@ def _memcpy_d2h(dst: int, src: int, nbytes: int) -> None:
         raise HsmuError(3, "cudaMemcpy failed (%d)" % rc)
 
 
+def _rows_from_device(rp: np.ndarray, col_ptr: int, val_ptr: int, rows):
+    """(local row_ptr, col, val) of the listed rows of a device CSR whose row
+    pointers (int32 or int64) are already on the host."""
+    rows = np.asarray(rows, dtype=np.int64)
+    lens = (rp[rows + 1] - rp[rows]).astype(np.int64)
+    lrp = np.zeros(rows.size + 1, dtype=np.int64)
+    np.cumsum(lens, out=lrp[1:])
+    col = np.empty(int(lrp[-1]), dtype=np.int32)
+    val = np.empty(int(lrp[-1]), dtype=np.float64)
+    i = 0
+    while i < rows.size:
+        j = i + 1
+        while j < rows.size and rows[j] == rows[j - 1] + 1:
+            j += 1
+        e0, e1 = int(rp[rows[i]]), int(rp[rows[j - 1] + 1])
+        o = int(lrp[i])
+        if e1 > e0:
+            _memcpy_d2h(col.ctypes.data + 4 * o, col_ptr + 4 * e0, 4 * (e1 - e0))
+            _memcpy_d2h(val.ctypes.data + 8 * o, val_ptr + 8 * e0, 8 * (e1 - e0))
+        i = j
+    return lrp, col, val
+
+
 def _stream_ptr(stream):
     if stream is None:
         torch = _torch()
@@ -307,6 +346,17 @@ class DeviceCSR64:
     @property
     def nnz(self):
         return self.desc.nnz
+
+    def row_ptr_host(self) -> np.ndarray:
+        """C's row pointers (int64[M+1]) copied to the host."""
+        rp = np.empty(self.M + 1, dtype=np.int64)
+        _memcpy_d2h(rp.ctypes.data, self.desc.row_ptr, rp.nbytes)
+        return rp
+
+    def rows_to_host(self, rows, row_ptr=None):
+        """Only the listed rows on the host: (local row_ptr int64[k+1], col, val)."""
+        rp = self.row_ptr_host() if row_ptr is None else row_ptr
+        return _rows_from_device(rp, self.desc.col, self.desc.val, rows)
 
     def to_host(self, stream=None):
         """(row_ptr int64, col int32, val float64) numpy arrays"""
@@ -354,11 +404,11 @@ class Engine:
             pass
 
     def spgemm_learned(self, A: DeviceCSR, B: DeviceCSR, params, margin: float, *, arith: int = 0,
-                       validate: bool = False, stream=None, stats: bool = False) -> DeviceCSR:
+                       validate: bool = False, stream=None, stats: bool = False, wait_polls: int = 0) -> DeviceCSR:
         """C = A * B with predicted row slots (hsmu_spgemm_learned); params: device float tensor."""
         L = load_library()
         C = c_csr()
-        o = c_opts(int(validate), int(arith), 0)
+        o = c_opts(int(validate), int(arith), 0, 0, int(wait_polls))
         m = c_mlp(params.data_ptr(), float(margin), 0)
         st = c_stats()
         rc = L.hsmu_spgemm_learned(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc), ctypes.byref(C),
@@ -387,11 +437,14 @@ class Engine:
         return n[:A.M]
 
     def spgemm(self, A: DeviceCSR, B: DeviceCSR, *, validate: bool = False, arith: int = 0,
-               tiles: BTiles | None = None, stream=None, stats: bool = False) -> DeviceCSR:
-        """C = A * B on the device (hsmu_spgemm / hsmu_spgemm_tiled)."""
+               tiles: BTiles | None = None, stream=None, stats: bool = False, wait_polls: int = 0,
+               tile_store: bool = True) -> DeviceCSR:
+        """C = A * B on the device (hsmu_spgemm / hsmu_spgemm_tiled).  wait_polls: the
+        test hook of hsmu_opts (bounded device waits give up after that many polls);
+        tile_store=False: the structure pass repeats the large rows' OR walk."""
         L = load_library()
         C = c_csr()
-        o = c_opts(int(validate), int(arith), 0)
+        o = c_opts(int(validate), int(arith), 0, 0, int(wait_polls), int(not tile_store))
         st = c_stats()
         sp = ctypes.byref(st) if stats else None
         if tiles is None:
@@ -490,13 +543,14 @@ class Batch:
     kind BATCH_PRODUCT: C_p = A[p] * B[p]; BATCH_GALERKIN: C_p = Pt[p] * (A[p] * B[p]).
     Results are views into the batch's output pool (valid while the batch lives)."""
 
-    def __init__(self, engine: "Engine", kind: int, A, B, Pt=None, arith: int = 0, stream=None):
+    def __init__(self, engine: "Engine", kind: int, A, B, Pt=None, arith: int = 0, stream=None,
+                 wait_polls: int = 0):
         n = len(A)
         self._keep = (list(A), list(B), list(Pt) if Pt is not None else None)
         arrA = (c_csr * n)(*[x.desc for x in A])
         arrB = (c_csr * n)(*[x.desc for x in B])
         arrP = (c_csr * n)(*[x.desc for x in Pt]) if Pt is not None else None
-        o = c_opts(0, int(arith), 0)
+        o = c_opts(0, int(arith), 0, 0, int(wait_polls))
         h = ctypes.c_void_p()
         _check(load_library().hsmu_batch_create(engine.handle, kind, n, arrA, arrB, arrP, ctypes.byref(o),
                                                 ctypes.byref(h), _stream_ptr(stream)), "hsmu_batch_create")
@@ -559,6 +613,20 @@ def selftest_dmul(n: int = 1 << 24, seed: int = 1) -> int:
     _check(load_library().hsmu_selftest_dmul(n, seed, ctypes.byref(out), _stream_ptr(None)),
            "hsmu_selftest_dmul")
     return int(out.value)
+
+
+def debug_fail_alloc(nth: int) -> None:
+    """Test hook: the nth device allocation from now on fails (0 disarms)."""
+    _check(load_library().hsmu_debug_fail_alloc(int(nth)), "hsmu_debug_fail_alloc")
+
+
+def probe_fp64_rate(iters: int = 8192, stream=None) -> float:
+    """FP64 lane operations per second of the device's FP64 pipe (rounded
+    multiply and add chains over a full grid; hsmu_probe_fp64_rate)."""
+    out = ctypes.c_double(0.0)
+    _check(load_library().hsmu_probe_fp64_rate(iters, ctypes.byref(out), _stream_ptr(stream)),
+           "hsmu_probe_fp64_rate")
+    return float(out.value)
 
 
 def spgemm_host(A: CSR, B: CSR, engine: Engine | None = None, **kw) -> CSR:

@@ -100,7 +100,16 @@ typedef struct hsmu_opts {
     int32_t window_cap;   /* 0: default slots per numeric window (<= 4096) */
     int32_t panels;       /* hsmu_spgemm_host: row panels of the copy pipeline (0: one per 32 MB
                            * of output; at most 8), sized in a decreasing geometric series */
-    int32_t reserved[4];
+    int32_t wait_polls;   /* test hook, 0 in normal use.  > 0: every bounded device wait of the call
+                           * gives up after this many polls instead of its default limit (the value
+                           * pass's wait for a window's column copy polls without blocking; the batch's
+                           * grid barriers spin this many times) and the call reports
+                           * HSMU_ERR_TIMEOUT.  A wait that gives up still lets its own copy land
+                           * before the kernel returns; the handle stays usable.  For hsmu_batch_create
+                           * it applies to every launch of the batch. */
+    int32_t no_tile_store; /* 1: the count pass keeps no C tiles of the large rows, and the structure
+                           * pass repeats their OR walk over B's tiles (same output; less scratch) */
+    int32_t reserved[2];
 } hsmu_opts;
 
 /* Per-call statistics (filled by hsmu_spgemm when stats != NULL). */
@@ -116,7 +125,7 @@ typedef struct hsmu_stats {
     float ms_numeric;        /* value accumulation */
     float ms_total;
     int32_t launches;        /* kernels this call launched */
-    int32_t reserved;
+    int32_t routed;          /* learned path: 1 when it handed the product to the plain path */
     int64_t spec_capacity;   /* learned path: entries of the speculative slots */
     int64_t fallback_rows;   /* learned path: rows that exceeded their slot and were redone */
 } hsmu_stats;
@@ -303,6 +312,21 @@ int hsmu_gen_aggregation(int side, hsmu_csr *P, hsmu_csr *Pt, void *stream);
  * number of results that differ in any bit (expected 0).  No reference
  * counterpart: the reference multiplies on the FP64 pipe only. */
 int hsmu_selftest_dmul(uint64_t n, uint64_t seed, uint64_t *mismatches, void *stream);
+
+/* Measures the device's FP64 pipe: every thread of a full grid runs
+ * independent chains of rounded multiplies and adds (the two operations a
+ * product costs in the value pass) for `iters` steps; stores FP64 lane
+ * operations per second (timed with CUDA events on `stream`).  The
+ * denominator of the value pass's FP64 roofline.  No reference counterpart. */
+int hsmu_probe_fp64_rate(int iters, double *lane_ops_per_s, void *stream);
+
+/* Test hook for the failure paths: the nth device allocation the library makes
+ * from now on (1 = the next one, counted across all calls and threads) fails
+ * as if the device were out of memory, so the call that makes it returns
+ * HSMU_ERR_ALLOC after releasing what it holds.  0 disarms the hook.
+ * No reference counterpart (the reference throws on a failed cudaMalloc,
+ * inc/cuda_comm.h:16-29). */
+int hsmu_debug_fail_alloc(int64_t nth);
 
 #ifdef __cplusplus
 }

@@ -26,13 +26,48 @@
 #define HSMU_NHC_COMPAT_H
 
 #include <cuda_runtime.h>
+/* the standard headers the reference's header chain gives its callers
+ * (inc/NHC_spgemm.h:1-8): its driver uses gettimeofday, std::ifstream and
+ * printf without including them itself (src/test.cu:24-51) */
+#include <limits.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <sys/time.h>
+#include <time.h>
 
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <fstream>
+#include <iostream>
+#include <string>
 
 #include "hsmu_gb.h"
+
+/* configuration macros of inc/NHC_spgemm.h that callers test
+ * (inc/NHC_spgemm.h:40,60-64; used by src/test.cu:40,71,74,84,88):
+ * test_NHC selects the NHC_spgemm call, AAT the driver's host transpose of A,
+ * CHECK_RESULT its cuSPARSE cross-check; threshold_value_selected is the
+ * column count below which the reference took its small-matrix path (this
+ * engine has one path for every size, so it only keeps the driver's own
+ * branches working) */
+#ifndef threshold_value_selected
+#define threshold_value_selected 4096
+#endif
+#ifndef test_NHC
+#define test_NHC 1
+#endif
+#ifndef AAT
+#define AAT 0
+#endif
+#ifndef CHECK_RESULT
+#define CHECK_RESULT 0
+#endif
+#ifndef SPGEMM_TRI_NUM
+#define SPGEMM_TRI_NUM 1
+#endif
 
 #ifndef value_t
 #define value_t double

@@ -17,7 +17,8 @@ import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = "/root/reference"
+# the read-only reference checkout; HSMU_REFERENCE_TREE names another location
+REF_TREE = os.environ.get("HSMU_REFERENCE_TREE", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 BIN = os.path.join(OUT, "ref_harness")
 

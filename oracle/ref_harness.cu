@@ -4,7 +4,7 @@
 // sources (staged into oracle/_ref/, never committed) and driven by
 // oracle/ref_run.py.  Nothing in the engine links or calls it.
 //
-// usage: ref_harness A.bin B.bin|same C.bin reps
+// usage: ref_harness A.bin B.bin|same C.bin|none reps   (none: time only, C is not written)
 //   *.bin: int32 M, N, nnz, then int32 row_ptr[M+1], int32 col[nnz], f64 val[nnz]
 // The call sequence mirrors the reference's driver (src/test.cu:62-91):
 // HtD_value_col_ptr on A and B, NHC_spgemm, then the release functions; the
@@ -93,7 +93,7 @@ int main(int argc, char **argv) {
         printf("HARNESS_CALL_MS %.6f nnz %d err %d\n", ms, C.nnz, (int)err);
         fflush(stdout);
         if (err != cudaSuccess) rc = 5;
-        if (r == reps - 1 && err == cudaSuccess) {
+        if (r == reps - 1 && err == cudaSuccess && strcmp(argv[3], "none") != 0) {
             std::vector<int> rp(C.M + 1), col(C.nnz > 0 ? C.nnz : 1);
             std::vector<double> val(C.nnz > 0 ? C.nnz : 1);
             cudaMemcpy(rp.data(), C.d_ptr, sizeof(int) * (C.M + 1), cudaMemcpyDeviceToHost);

@@ -40,12 +40,13 @@ def _read(path):
     return CSR(M, N, rp, col, val)
 
 
-def run(A, B=None, reps: int = 2, timeout: float = 1800.0):
+def run(A, B=None, reps: int = 2, timeout: float = 1800.0, output: bool = True):
     """C = A*B with the reference (B=None: a second copy of A, as its driver
     does for C = A*A).  Returns (C, info) with info = {call_ms: [...],
     time2_ms: [...], conversion_ms: [...]} -- time2 is the reference's own
     timed region (symbolic + allocation + columns + values, no setup or B
-    conversion, src/compressed/compressed_NHC_spgemm.cu:35-202)."""
+    conversion, src/compressed/compressed_NHC_spgemm.cu:35-202).  output=False
+    only times the calls (C is None): nothing is copied back or written."""
     if not available():
         raise FileNotFoundError(BIN)
     with tempfile.TemporaryDirectory() as td:
@@ -57,7 +58,7 @@ def run(A, B=None, reps: int = 2, timeout: float = 1800.0):
         cwd = os.path.join(td, "w", "x")
         os.makedirs(cwd)
         os.makedirs(os.path.join(td, "data"))
-        r = subprocess.run([BIN, a, b if B is not None else "same", c, str(reps)], cwd=cwd,
+        r = subprocess.run([BIN, a, b if B is not None else "same", c if output else "none", str(reps)], cwd=cwd,
                            capture_output=True, text=True, timeout=timeout)
         out = r.stdout
         if r.returncode != 0:
@@ -69,4 +70,4 @@ def run(A, B=None, reps: int = 2, timeout: float = 1800.0):
             "conversion_ms": [float(x) for x in
                               re.findall(r"the run time for Initialize_compressed_mask64_matrix is ([0-9.]+)", out)],
         }
-        return _read(c), info
+        return (_read(c) if output else None), info

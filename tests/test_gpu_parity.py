@@ -260,3 +260,30 @@ def test_invalid_arith_rejected(engine):
     A = gen.laplacian2d(8, seed=0)
     with pytest.raises(hsmu_gb.HsmuError):
         run(engine, A, A, arith=3)
+
+
+@pytest.mark.parametrize("case", ["rmat15", "rmat14T", "chunked"])
+def test_tile_store_and_or_walk_give_the_same_bits(engine, case):
+    # the large rows' structure from the count pass's stored tiles, or from a second
+    # OR walk over B's tiles: identical output
+    import hsmu_gb
+
+    if case == "rmat15":
+        A = B = gen.rmat(15, 16, seed=2)
+    elif case == "rmat14T":
+        A = gen.rmat(14, 16, seed=3)
+        B = gen.transpose(A)
+    else:
+        A = gen.poisson_random(400, 40, seed=7, ncols=2000)
+        B = gen.poisson_random(2000, 60, seed=8, ncols=1_200_000)
+    dA = hsmu_gb.DeviceCSR.from_host(A)
+    dB = dA if B is A else hsmu_gb.DeviceCSR.from_host(B)
+    C1 = engine.spgemm(dA, dB, stats=True).to_host()
+    assert engine.last_stats["windows"] > 0
+    C2 = engine.spgemm(dA, dB, tile_store=False).to_host()
+    np.testing.assert_array_equal(C1.row_ptr, C2.row_ptr)
+    np.testing.assert_array_equal(C1.col, C2.col)
+    assert np.array_equal(C1.val.view(np.int64), C2.val.view(np.int64))
+    rp, col, val = oracle.spgemm(A, B)
+    np.testing.assert_array_equal(C1.col, col)
+    assert np.array_equal(C1.val.view(np.int64), val.view(np.int64))
