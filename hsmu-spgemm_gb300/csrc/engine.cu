@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <initializer_list>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -47,9 +48,13 @@ struct hsmu_handle_s {
     int device;
     int nsm;
     Ctl *h_ctl;  // pinned host mirror of the control block
-    Ctl *h_mid;  // pinned mirror read after the bounds pass (tile store size)
-    cudaEvent_t ev_mid;
     cudaEvent_t ev[8];
+    // tile store arena (C tiles of the large rows, kept by the count pass): grown, up to
+    // STORE_MAX_TILES, to the largest need a call has reported, before the next call
+    int *arena_col;
+    unsigned long long *arena_mask;
+    long long *arena_info;
+    long long arena_cap, arena_want;
     // host-buffer entry: copy streams and their ordering events
     cudaStream_t cs_in, cs_out;
     cudaEvent_t ev_in, ev_panel, ev_out;
@@ -96,9 +101,9 @@ int err_from_dev(int err) { return status_from_dev_err(err); }
 // C's column array: 4 ints of slack past nnz, so that the value pass can fetch a
 // window's columns in 16-byte units with bulk copies
 constexpr size_t COL_PAD = 4;
-// largest tile store (12 bytes per tile: 16 GB); beyond it the structure pass
-// repeats the large rows' OR walk instead
-constexpr long long STORE_MAX_TILES = (16ll << 30) / 12;
+// largest tile store arena (20 bytes per tile: 16 GB); rows beyond it are built
+// by the structure pass's own OR walk instead
+constexpr long long STORE_MAX_TILES = (16ll << 30) / 20;
 
 bool csr_ok(const hsmu_csr *X) {
     if (!X || X->M < 0 || X->N < 0 || X->nnz < 0) return false;
@@ -130,6 +135,20 @@ void pfree(T *&p, cudaStream_t st) {
 }
 
 int grid_rows(const hsmu_handle_s *h) { return h->nsm * 8; }
+
+// arrays the library allocated from the stream-ordered pool and handed to the caller:
+// returned to the pool once every stream of the device is done with them (the free
+// functions take no stream; a plain cudaFree measured not to give the bytes back to
+// the pool's in-use count)
+void free_owned(std::initializer_list<const void *> ptrs) {
+    bool any = false;
+    for (const void *p : ptrs) any |= p != nullptr;
+    if (!any) return;
+    cudaDeviceSynchronize();
+    for (const void *p : ptrs)
+        if (p) cudaFreeAsync(const_cast<void *>(p), 0);
+    cudaStreamSynchronize(0);
+}
 
 // B -> tiles into caller-visible arrays (tile arrays sized by nnz(B) >= tiles)
 int build_tiles(hsmu_handle_s *h, const hsmu_csr *B, hsmu_btiles *out, Ctl *ctl, int validate, cudaStream_t st,
@@ -209,11 +228,15 @@ struct PlainRun {
     Ctl *ctl = nullptr;
     Ctl hc{};
     int launches = 0;
-    // C tiles of the large rows, kept by the count pass for the structure pass
+    // C tiles of the large rows, kept by the count pass for the structure pass (in the
+    // handle's arena; per-row offsets and counts here)
     long long *ts_off = nullptr;
-    int *ts_cnt = nullptr, *ts_col = nullptr;
-    unsigned long long *ts_mask = nullptr;
+    int *ts_cnt = nullptr, *ts_nwin = nullptr, *ts_wbase = nullptr;
     bool have_store = false;
+    // the count pass reserves the large rows' windows (one product, one panel of
+    // structure + values); the row panels of the host-buffer path restart the window
+    // buffer at 0 for every panel and reserve them in the structure pass instead
+    bool reserve_windows = true;
 
     PlainRun(hsmu_handle_s *h_, cudaStream_t st_, const hsmu_opts &o_) : h(h_), st(st_), o(o_) {}
     ~PlainRun() { release(); }
@@ -246,8 +269,9 @@ struct PlainRun {
     }
 
     // B's tiles (built, or the caller's) and the bounds pass: products, tile span and class
-    // of every row of A, the class bins; with `store`, also the tile store's row offsets,
-    // whose total is read back (overlapped with the next kernels) by count_scan
+    // of every row of A, the class bins; with `store`, also every large row's tile bound
+    // and the per-row arrays of the tile store (the arena is grown here when the previous
+    // call needed more than it had)
     int tiles_bounds(const hsmu_csr *B, const hsmu_btiles *Bt_in, bool count_tiles, cudaEvent_t ev_tiles,
                      bool store) {
         if (Bt_in) {
@@ -269,49 +293,58 @@ struct PlainRun {
         CKR(palloc(&ri.cnnz, (size_t)M + 1, st));
         CKR(palloc(&scan_tmp, scan_tmp_ints(M), st));
         if (store) {
+            CKR(grow_arena());
             CKR(palloc(&ri.tcap, (size_t)M, st));
-            CKR(palloc(&ts_off, (size_t)M + 1, st));
+            if (h->arena_cap > 0) {
+                CKR(palloc(&ts_off, (size_t)M, st));
+                CKR(palloc(&ts_cnt, (size_t)M, st));
+                CKR(palloc(&ts_nwin, (size_t)M, st));
+                if (reserve_windows) CKR(palloc(&ts_wbase, (size_t)M, st));
+                have_store = true;
+            }
         }
         launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
         launches += 6;  // bounds + binning
-        if (store) {
-            launch_scan64(ri.tcap, ts_off, M, &ctl->store_tiles, scan_tmp, st);
-            launches += 3;
-            CKR(cudaMemcpyAsync(h->h_mid, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-            CKR(cudaEventRecord(h->ev_mid, st));
-        }
         CKR(cudaGetLastError());
         return HSMU_OK;
     }
 
-    // exact count of every row (the large rows' tiles kept in the store when it fits),
+    cudaError_t grow_arena() {
+        if (h->arena_want <= h->arena_cap) return cudaSuccess;
+        const long long want = std::min(h->arena_want, STORE_MAX_TILES);
+        pfree(h->arena_col, st);
+        pfree(h->arena_mask, st);
+        pfree(h->arena_info, st);
+        h->arena_cap = 0;
+        cudaError_t e = palloc(&h->arena_col, (size_t)want, st);
+        if (e == cudaSuccess) e = palloc(&h->arena_mask, (size_t)want, st);
+        if (e == cudaSuccess) e = palloc(&h->arena_info, (size_t)want, st);
+        if (e != cudaSuccess) {
+            pfree(h->arena_col, st);
+            pfree(h->arena_mask, st);
+            pfree(h->arena_info, st);
+            h->arena_want = 0;
+            return e;
+        }
+        h->arena_cap = want;
+        return cudaSuccess;
+    }
+
+    // exact count of every row (the large rows' tiles kept in the arena while it lasts),
     // scan into C's row pointers and nnz(C), one host read
     int count_scan(int32_t *host_rp) {
         CKR(palloc(&crp, (size_t)M + 1, st));
         launch_count_small(Ad, Bd, Btd, ri, ctl, h->nsm, st);
-        launches += 2;
-        TileStore tsd{};
-        if (ri.tcap) {
-            // bounds are done once ev_mid has passed; the small rows' count runs meanwhile
-            CKR(cudaEventSynchronize(h->ev_mid));
-            const Ctl m = *h->h_mid;
-            if (m.err) return err_from_dev(m.err);
-            if (m.bin_count[BIN_L] > 0 && m.store_tiles > 0 && m.store_tiles <= STORE_MAX_TILES) {
-                CKR(palloc(&ts_cnt, (size_t)M, st));
-                CKR(palloc(&ts_col, (size_t)m.store_tiles, st));
-                CKR(palloc(&ts_mask, (size_t)m.store_tiles, st));
-                tsd = TileStore{ts_off, ts_cnt, ts_col, ts_mask};
-                have_store = true;
-            }
-        }
+        const TileStore tsd = store_view();
         launch_count_large(Ad, Btd, ri, have_store ? &tsd : nullptr, ctl, h->nsm, st);
         launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
-        launches += 4;  // large-row count, scan 3
+        launches += 6;  // count 3, scan 3
         CKR(cudaGetLastError());
         CKR(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
         if (host_rp) CKR(cudaMemcpyAsync(host_rp, crp, sizeof(int32_t) * ((size_t)M + 1), cudaMemcpyDeviceToHost, st));
         CKR(cudaStreamSynchronize(st));
         hc = *h->h_ctl;
+        if (ri.tcap && hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;  // for the next call
         if (hc.err) return err_from_dev(hc.err);
         if (hc.nnz > INT_MAX) return HSMU_ERR_OVERFLOW;
         win_cap = (long long)hc.win_bound;
@@ -343,10 +376,16 @@ struct PlainRun {
         return HSMU_OK;
     }
 
+    TileStore store_view() const {
+        return TileStore{ts_off,        ts_cnt,       ts_nwin,       reserve_windows ? ts_wbase : nullptr,
+                         h->arena_col,  h->arena_mask, h->arena_info, h->arena_cap,
+                         (int)(hc.store_used <= h->arena_cap)};
+    }
+
     // sorted columns of rows lo..hi-1, values of warp-sized rows, numeric windows of the others
     void structure(int lo, int hi) {
         if (hc.nnz == 0) return;
-        const TileStore tsd{ts_off, ts_cnt, ts_col, ts_mask};
+        const TileStore tsd = store_view();
         launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_PLAIN, crp, nullptr, ccol, cval, nullptr, nullptr, lo, hi}, win,
                          win_cap, ctl, o.arith, h->nsm, st, hc.bin_count, have_store ? &tsd : nullptr);
         for (int b = 0; b < NBIN; b++) launches += hc.bin_count[b] > 0;
@@ -395,8 +434,8 @@ struct PlainRun {
         pfree(ri.tcap, st);
         pfree(ts_off, st);
         pfree(ts_cnt, st);
-        pfree(ts_col, st);
-        pfree(ts_mask, st);
+        pfree(ts_nwin, st);
+        pfree(ts_wbase, st);
         have_store = false;
         pfree(scan_tmp, st);
         pfree(win, st);
@@ -529,6 +568,7 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
         return HSMU_OK;
     };
     std::vector<int> cut;
+    r.reserve_windows = false;  // the output is written in row panels
     rc = upload(B, &dB);
     if (!rc) {
         if (same) dA = dB;
@@ -621,11 +661,14 @@ done:
 
 // Learned path (see learned.cu): predicted slots instead of the exact count pass.
 // B's tiles and the bounds pass are shared with the plain path (a PlainRun holds
-// them); one host read after the bounds pass decides the route: an input with no
-// row of the large class (every row takes the one-thread or one-warp path,
-// whose exact count costs about what the prediction does) has nothing for the
-// prediction to skip, so the plain path finishes it on the same tiles and
-// bounds.  Either way the output is the plain path's, bit for bit.
+// them).  What the prediction saves is the count pass of the rows that take
+// numeric windows (large rows, and warp rows above FUSE_CAP entries); for every
+// other row the exact count is about as cheap as the prediction, and filling
+// speculative slots costs a compaction copy.  So the plain path finishes the
+// product on the same tiles and bounds when every row is tiny (known after the
+// bounds pass), or when no row is large and none is predicted above FUSE_CAP
+// entries (known after the prediction).  Either way the output is the plain
+// path's, bit for bit.
 int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
                         const hsmu_opts *opts, cudaStream_t st, hsmu_stats *stats) {
     if (!h || !csr_ok(A) || !csr_ok(B) || !C || !model || !model->params) return HSMU_ERR_INVALID;
@@ -660,8 +703,29 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         rc = err_from_dev(hc.err);
         goto done;
     }
-    if (hc.bin_count[BIN_L] == 0) {
+    if (hc.bin_count[BIN_L] == 0 && hc.bin_count[BIN_DS] == 0) goto plain;
+    {
+        CK(palloc(&feat, (size_t)M, st));
+        CK(palloc(&cap, (size_t)M + 1, st));
+        CK(palloc(&soff, (size_t)M + 1, st));
+        launch_features(r.Ad, r.Bd, feat, nullptr, h->nsm, st);
+        launch_capacity(model->params, feat, r.ri.prod, M, B->N, model->margin, cap, h->nsm, st, &r.ctl->pred_wide);
+        launch_scan64(cap, soff, M, &r.ctl->nnz, r.scan_tmp, st);  // nnz field holds the slot total for now
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->h_ctl, r.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        hc = *h->h_ctl;
+        if (hc.err) {
+            rc = err_from_dev(hc.err);
+            goto done;
+        }
+        if (hc.bin_count[BIN_L] == 0 && hc.pred_wide == 0) goto plain;
+        goto learned;
+    }
+plain:
+    {
         // the plain path on the same tiles and bounds
+        CK(cudaMemsetAsync(&r.ctl->nnz, 0, sizeof(long long), st));
         rc = r.count_scan(nullptr);
         if (!rc && stats) cudaEventRecord(h->ev[2], st);
         if (!rc) rc = r.alloc_output();
@@ -690,28 +754,15 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         }
         goto done;
     }
+learned:
     {
         Ctl *ctl = r.ctl;
         const DevCSR &Ad = r.Ad, &Bd = r.Bd;
         const DevTiles &Btd = r.Btd;
         RowInfo &ri = r.ri;
-        CK(palloc(&feat, (size_t)M, st));
-        CK(palloc(&cap, (size_t)M + 1, st));
-        CK(palloc(&soff, (size_t)M + 1, st));
         CK(palloc(&flag, (size_t)M, st));
         CK(cudaMemsetAsync(flag, 0, (size_t)M, st));
-        launch_features(Ad, Bd, feat, nullptr, h->nsm, st);
-        launch_capacity(model->params, feat, ri.prod, M, B->N, model->margin, cap, h->nsm, st);
-        launch_scan64(cap, soff, M, &ctl->nnz, r.scan_tmp, st);  // nnz field holds the slot total for now
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        hc = *h->h_ctl;
         if (stats) cudaEventRecord(h->ev[2], st);
-        if (hc.err) {
-            rc = err_from_dev(hc.err);
-            goto done;
-        }
         spec_total = hc.nnz;
         win_cap = 2 * (long long)hc.win_bound;  // speculative pass + redo of overflowing rows
         if (win_cap > INT_MAX) {
@@ -994,17 +1045,13 @@ int hsmu_handle_create(hsmu_handle *out) {
         delete h;
         return HSMU_ERR_ALLOC;
     }
-    if (cudaMallocHost(reinterpret_cast<void **>(&h->h_mid), sizeof(Ctl)) != cudaSuccess) {
-        hsmu_handle_destroy(h);
-        return HSMU_ERR_ALLOC;
-    }
+
     for (auto &e : h->ev) cudaEventCreate(&e);
     if (cudaStreamCreateWithFlags(&h->cs_in, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->cs_out, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_mid, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess) {
         hsmu_handle_destroy(h);
         return HSMU_ERR_CUDA;
     }
@@ -1029,12 +1076,17 @@ int hsmu_handle_destroy(hsmu_handle h) {
     if (!h) return HSMU_OK;
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out, h->ev_mid})
+    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out})
         if (e) cudaEventDestroy(e);
+    if (h->arena_col || h->arena_mask || h->arena_info) {
+        cudaDeviceSynchronize();  // no call of this handle still reads the arena
+        for (void *p : {(void *)h->arena_col, (void *)h->arena_mask, (void *)h->arena_info})
+            if (p) cudaFreeAsync(p, 0);
+        cudaStreamSynchronize(0);
+    }
     for (cudaStream_t s : {h->cs_in, h->cs_out})
         if (s) cudaStreamDestroy(s);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
-    if (h->h_mid) cudaFreeHost(h->h_mid);
     delete h;
     return HSMU_OK;
 }
@@ -1067,11 +1119,7 @@ int hsmu_spgemm64(hsmu_handle h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr6
 
 int hsmu_csr64_free(hsmu_csr64 *C) {
     if (!C) return HSMU_ERR_INVALID;
-    if (C->owned) {
-        cudaFree(C->row_ptr);
-        cudaFree(C->col);
-        cudaFree(C->val);
-    }
+    if (C->owned) free_owned({C->row_ptr, C->col, C->val});
     std::memset(C, 0, sizeof(*C));
     return HSMU_OK;
 }
@@ -1115,10 +1163,7 @@ done:
 
 int hsmu_btiles_free(hsmu_btiles *t) {
     if (!t) return HSMU_ERR_INVALID;
-    cudaFree(t->tile_ptr);
-    cudaFree(t->tile_col);
-    cudaFree(t->mask);
-    cudaFree(t->tile_off);
+    free_owned({t->tile_ptr, t->tile_col, t->mask, t->tile_off});
     std::memset(t, 0, sizeof(*t));
     return HSMU_OK;
 }
@@ -1176,11 +1221,7 @@ done:
 
 int hsmu_csr_free(hsmu_csr *C) {
     if (!C) return HSMU_ERR_INVALID;
-    if (C->owned) {
-        cudaFree(C->row_ptr);
-        cudaFree(C->col);
-        cudaFree(C->val);
-    }
+    if (C->owned) free_owned({C->row_ptr, C->col, C->val});
     std::memset(C, 0, sizeof(*C));
     return HSMU_OK;
 }

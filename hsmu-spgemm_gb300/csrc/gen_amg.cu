@@ -130,9 +130,10 @@ extern "C" int hsmu_gen_poisson7(int side, hsmu_csr *A, void *stream) {
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) rc = HSMU_ERR_CUDA;
     }
     if (rc) {
-        cudaFree(rp);
-        if (col) cudaFree(col);
-        if (val) cudaFree(val);
+        cudaFreeAsync(rp, st);
+        if (col) cudaFreeAsync(col, st);
+        if (val) cudaFreeAsync(val, st);
+        cudaStreamSynchronize(st);
         return rc;
     }
     *A = hsmu_csr{n, n, nnz, 1, rp, col, val};
@@ -166,7 +167,8 @@ extern "C" int hsmu_gen_aggregation(int side, hsmu_csr *P, hsmu_csr *Pt, void *s
     }
     if (rc) {
         for (void *p : {(void *)prp, (void *)pcol, (void *)pval, (void *)trp, (void *)tcol, (void *)tval})
-            if (p) cudaFree(p);
+            if (p) cudaFreeAsync(p, st);
+        cudaStreamSynchronize(st);
         return rc;
     }
     *P = hsmu_csr{n, nc, n, 1, prp, pcol, pval};

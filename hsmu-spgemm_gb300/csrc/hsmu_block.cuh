@@ -198,26 +198,6 @@ __device__ __forceinline__ T block_excl_max1(T v, T *s_w, T ident) {
     return ex;
 }
 
-// exclusive max-scan with one barrier that also returns the block's maximum
-template <int NT, class T>
-__device__ __forceinline__ T block_excl_max1t(T v, T *s_w, T ident, T &total) {
-    const int lane = lane_id(), w = threadIdx.x >> 5;
-    const T incl = warp_incl_max(v);
-    T ex = __shfl_up_sync(FULL, incl, 1);
-    if (lane == 0) ex = ident;
-    if (lane == 31) s_w[w] = incl;
-    __syncthreads();
-    T tot = ident;
-#pragma unroll
-    for (int j = 0; j < NT / 32; j++) {
-        const T x = s_w[j];
-        if (j < w) ex = max(ex, x);
-        tot = max(tot, x);
-    }
-    total = tot;
-    return ex;
-}
-
 template <class T>
 __device__ __forceinline__ T warp_incl_max(T v) {
     const int lane = lane_id();

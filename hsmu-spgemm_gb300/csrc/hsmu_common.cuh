@@ -82,7 +82,9 @@ struct Ctl {
                                      // rows (bounds pass) + warp rows above FUSE_CAP (count pass)
     unsigned long long cur_bound_ds; // same for every warp row with more than FUSE_CAP products
                                      // (bounds pass; for paths without a count pass)
-    long long store_tiles;           // sum of RowInfo::tcap (entries of the tile store)
+    long long store_tiles;           // sum of RowInfo::tcap: arena entries the large rows could use
+    long long store_used;            // arena entries reserved by the count pass
+    int pred_wide;                   // learned path: rows predicted above FUSE_CAP entries
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -54,13 +54,21 @@ struct RowInfo {
 
 // C tiles of the large-class rows, kept by the count pass (which builds them
 // anyway) so that the structure pass streams each row's tile list instead of
-// repeating the OR walk over B's tiles.  Row i's list: tcol/tmask[off[i] ..
-// off[i] + cnt[i]), tile ids ascending; off is the scan of RowInfo::tcap.
+// repeating the OR walk over B's tiles.  Each large row reserves RowInfo::tcap
+// entries of the arena (tcol/tmask, `cap` entries, owned by the handle) with
+// one atomic; a row that finds the arena full keeps nothing (cnt[i] = -1) and
+// the structure pass walks B for it as before.  Row i's list:
+// tcol/tmask[off[i] .. off[i] + cnt[i]), tile ids ascending.
 struct TileStore {
-    const long long *off;       // [M+1]
-    int *cnt;                   // [M] tiles stored per row
-    int *tcol;                  // tile ids
-    unsigned long long *tmask;  // column masks
+    long long *off;             // [M] written by the count pass
+    int *cnt;                   // [M] tiles stored per row, -1: none
+    int *nwin;                  // [M] numeric windows of the row (rows with a list)
+    int *wbase;                 // [M] index of the row's first window (reserved by the count pass)
+    int *tcol;                  // arena: tile ids
+    unsigned long long *tmask;  // arena: column masks
+    long long *tinfo;           // arena: first slot | (window ordinal + 1) << 32 (hsmu_tilelist.cuh)
+    long long cap;              // arena entries
+    int all_stored;             // host: every large row got a list (no OR-walk rows left)
 };
 
 // scratch ints of RowInfo::bin_cnt for M rows
@@ -85,8 +93,9 @@ void launch_scan64(const int *in, long long *out, int n, long long *total64, int
 
 // learned.cu
 void launch_features(const DevCSR &A, const DevCSR &B, float4 *feat, long long *prod_out, int nsm, cudaStream_t st);
+// wide (nullable): incremented for every row whose slot exceeds FUSE_CAP entries
 void launch_capacity(const float *params, const float4 *feat, const long long *prod, int M, int N, float margin,
-                     int *cap, int nsm, cudaStream_t st);
+                     int *cap, int nsm, cudaStream_t st, int *wide = nullptr);
 void launch_compact(int M, const long long *soff, const int *crp, const unsigned char *flag, const int *scol,
                     const double *sval, int *ccol, double *cval, int nsm, cudaStream_t st);
 
@@ -94,7 +103,7 @@ void launch_compact(int M, const long long *soff, const int *crp, const unsigned
 void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
                   cudaStream_t st);
 // the same in two launches: rows of the tiny and warp classes, then the large class
-// (ts: nullable; when given, every large row's C tiles are stored)
+// (ts: nullable; when given, the large rows' C tiles are stored while the arena lasts)
 void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
                         cudaStream_t st);
 void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,

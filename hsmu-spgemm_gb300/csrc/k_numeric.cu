@@ -63,15 +63,24 @@ static_assert(NUM_CTAS_PER_SM * (NUM_WARPS * sizeof(NumSmem) + 1024) <= 228 * 10
 static_assert(WIN_CAP * 8 >= (WIN_CAP + 8) * 4, "column stage fits in the accumulator");
 
 // A entries of each window's row (0 past the emitted windows), scanned into
-// the windows' offsets in the cursor array
-__global__ void __launch_bounds__(256) k_win_len(const Window *__restrict__ win, int win_cap,
-                                                 const int *__restrict__ arp, const Ctl *ctl, int *__restrict__ len) {
+// the windows' offsets in the cursor array.  A window written with a slot
+// count of 0 (the large rows built from their stored tiles) gets its count
+// here: up to the next window's first slot when that window continues the
+// same row, else up to the row's end.
+__global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int win_cap, const int *__restrict__ arp,
+                                                 const int *__restrict__ crp, const Ctl *ctl, int *__restrict__ len) {
     const int nwin = min(ctl->win_count, win_cap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < win_cap; w += gridDim.x * blockDim.x) {
         int n = 0;
         if (w < nwin) {
             const int row = win[w].row;
             n = arp[row + 1] - arp[row];
+            if (win[w].cnt == 0) {
+                const int s0 = win[w].s0;
+                int e = crp[row + 1] - crp[row];
+                if (w + 1 < nwin && win[w + 1].row == row && win[w + 1].s0 > s0) e = win[w + 1].s0;
+                win[w].cnt = e - s0;
+            }
         }
         len[w] = n;
     }
@@ -79,7 +88,12 @@ __global__ void __launch_bounds__(256) k_win_len(const Window *__restrict__ win,
 
 // cursor of (window w, A entry p of its row): index of the first entry of B row
 // acol[p] whose column lies in or after the window's first tile -- found in
-// B's sorted tile list, whose tile_off gives the tile's first entry
+// B's sorted tile list, whose tile_off gives the tile's first entry.  One warp
+// per window, all pairs in flight at once.  (Seeding each window's search from
+// the previous window of the same row -- a warp taking 8 consecutive windows,
+// one binary search and then forward gallops per A entry -- was measured
+// slower: R-MAT 18 value stage 28.1 -> 30.4 ms, the chained gallops of a heavy
+// row's group form a tail and fewer searches run at once.)
 __global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ win, int win_cap,
                                                      const long long *__restrict__ woff, long long cur_cap,
                                                      const int *__restrict__ arp, const int *__restrict__ acol,
@@ -318,7 +332,7 @@ void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const 
                     int wait_polls) {
     if (win_cap <= 0) return;
     cudaMemsetAsync(&ctl->win_next, 0, sizeof(int), st);
-    k_win_len<<<nsm * 4, 256, 0, st>>>(win, (int)win_cap, A.rp, ctl, wc.len);
+    k_win_len<<<nsm * 4, 256, 0, st>>>(const_cast<Window *>(win), (int)win_cap, A.rp, crp, ctl, wc.len);
     launch_scan64(wc.len, wc.off, (int)win_cap, wc.total, wc.scan_tmp, st);
     k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
                                             Bt.off, wc.cur, ctl);

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     __shared__ int s_cnt[NBIN];
     const int sub = threadIdx.x & (G - 1);
     const int rloc = threadIdx.x / G;
-    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0;
+    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0, my_tc = 0;
     if (threadIdx.x < NBIN) s_cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int rb = blockIdx.x * RPB; rb < M; rb += gridDim.x * RPB) {
@@ -83,7 +83,9 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
             if (ri.tcap) {
                 // a large row has at most one C tile per tile of its span and per B tile it reads
                 const long long span = prod ? (long long)(tmax - tmin + 1) : 0;
-                ri.tcap[i] = bin == BIN_L ? (int)(tsum < span ? tsum : span) : 0;
+                const int tc = bin == BIN_L ? (int)(tsum < span ? tsum : span) : 0;
+                ri.tcap[i] = tc;
+                my_tc += (unsigned long long)tc;
             }
         }
     }
@@ -93,7 +95,9 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     my_wb = warp_sum(my_wb);
     my_cb = warp_sum(my_cb);
     my_cbd = warp_sum(my_cbd);
+    my_tc = warp_sum(my_tc);
     if (lane_id() == 0) {
+        if (my_tc) atomicAdd(reinterpret_cast<unsigned long long *>(&ctl->store_tiles), my_tc);
         if (my_prod) atomicAdd(&ctl->products, my_prod);
         if (my_wb) atomicAdd(&ctl->win_bound, my_wb);
         if (my_cb) atomicAdd(&ctl->cur_bound, my_cb);

@@ -33,6 +33,7 @@
 #include "hsmu_kernels.h"
 #include "hsmu_products.cuh"
 #include "hsmu_rowops.cuh"
+#include "hsmu_tilelist.cuh"
 
 namespace hsmu {
 
@@ -263,13 +264,15 @@ struct SlSmem {
     int wt[SL_WL];
 };
 
+// stored: nullable per-row tile-list counts of the tile store; rows that have a
+// list (>= 0) are built by k_struct_ls and skipped here
 __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__restrict__ arp,
                                                          const int *__restrict__ acol,
                                                          const int *__restrict__ tptr,
                                                          const int *__restrict__ tcol,
                                                          const unsigned long long *__restrict__ tmask, RowInfo ri,
                                                          RowOut out, Window *__restrict__ win, long long win_cap,
-                                                         Ctl *ctl) {
+                                                         const int *__restrict__ stored, Ctl *ctl) {
     extern __shared__ unsigned long long s_dyn[];
     SlSmem &S = *reinterpret_cast<SlSmem *>(s_dyn);
     // warp totals of the three block scans of a chunk (one array each: one barrier per scan)
@@ -284,7 +287,7 @@ __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__
     int *__restrict__ ccol = out.ccol;
     for (int r = b0 + blockIdx.x; r < b1; r += gridDim.x) {
         const int i = rows[r];
-        if (skip_row(out, i)) continue;
+        if (skip_row(out, i) || (stored && stored[i] >= 0)) continue;
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
         const int a_lo = arp[i], a_hi = arp[i + 1];
         const long long rowbase = out_base(out, i);
@@ -393,29 +396,24 @@ __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__
     }
 }
 
-// ---- large rows from their stored C tiles (PLAIN mode, tile store present)
-// The count pass kept every large row's non-empty C tiles (ascending ids and
-// masks), so the row needs no second OR walk over B: the CTA streams the list
-// NT tiles at a time -- slot of each tile (block scan of popcounts), window key
-// (block max-scan), window starts (block scan) -- twice: the first pass counts
-// the row's windows so that one atomic reserves them contiguously (the value
-// pass relies on a row's windows being neighbours), the second writes the
-// windows and the columns (lane per tile, lowest bit first).  Windows are cut
-// where the tile's first slot crosses a multiple of WIN_CUT, its rank crosses a
-// multiple of WIN_TCAP, or its offset from the row's first tile crosses a
-// multiple of WIN_SPAN -- the limits of k_numeric's tables.
+// ---- large rows from their stored C tile lists (PLAIN mode, tile store present)
+// The count pass kept every large row's non-empty C tiles in column order,
+// each with its first slot in the row and, for a tile that starts a numeric
+// window, the window's ordinal (hsmu_tilelist.cuh).  So the row needs neither
+// a second OR walk over B nor any scan: every warp takes 32 consecutive tiles
+// at a time, writes the windows they start (slot count left 0: the window
+// length pass derives it from the next window's first slot, the row's windows
+// being neighbours) and the tiles' columns -- each store of the warp covers
+// consecutive entries of the row.  The row's windows were reserved by the
+// count pass (ts.wbase); without that (row panels, whose windows restart at 0
+// for every panel) one atomic per row reserves them here.
 constexpr int SLS_THREADS = 256;
 
-__device__ __forceinline__ long long win_key_row(int slot, int rank, int toff) {
-    return ((long long)(slot / WIN_CUT) << 40) | ((long long)(rank / WIN_TCAP) << 20) | (long long)(toff / WIN_SPAN);
-}
-
-__global__ void __launch_bounds__(SLS_THREADS) k_struct_ls(int M, RowInfo ri, TileStore ts, RowOut out,
+__global__ void __launch_bounds__(SLS_THREADS, 6) k_struct_ls(int M, RowInfo ri, TileStore ts, RowOut out,
                                                            Window *__restrict__ win, long long win_cap, Ctl *ctl) {
     constexpr int NT = SLS_THREADS;
-    __shared__ int s_slot[NT / 32], s_st[NT / 32];
-    __shared__ long long s_key[NT / 32];
     __shared__ int s_wbase;
+    const int lane = lane_id(), w = threadIdx.x >> 5;
     const int *rows = ri.bins + (size_t)BIN_L * M;
     int b0, b1;
     bin_slice(rows, ctl->bin_count[BIN_L], out, M, b0, b1);
@@ -424,82 +422,42 @@ __global__ void __launch_bounds__(SLS_THREADS) k_struct_ls(int M, RowInfo ri, Ti
         const int i = rows[r];
         if (skip_row(out, i)) continue;
         const int n = ts.cnt[i];
+        if (n < 0) continue;  // no list kept (the arena was full): k_struct_l builds this row
         const long long sb = ts.off[i];
-        const int tmin = ri.tmin[i];
+        const int nwin = ts.nwin[i];
         const long long rowbase = out.crp[i];
         const int nnz = out.crp[i + 1] - out.crp[i];
-        int wbase = 0, nwin = 0;
-        for (int pass = 0; pass < 2; pass++) {
-            int run = 0, wrun = 0;
-            long long carry = -1;
-            for (int blk = 0; blk < n; blk += NT) {
-                const int q = blk + (int)threadIdx.x;
+        int wbase;
+        if (ts.wbase) {
+            wbase = ts.wbase[i];
+        } else {
+            if (threadIdx.x == 0) s_wbase = atomicAdd(&ctl->win_count, nwin);
+            __syncthreads();
+            wbase = s_wbase;
+        }
+        if (wbase >= 0 && (long long)wbase + nwin <= win_cap) {
+            for (int q0 = w * WARP; q0 < n; q0 += NT) {
+                const int q = q0 + lane;
                 const bool v = q < n;
                 const int t = v ? __ldg(ts.tcol + sb + q) : 0;
                 const unsigned long long m = v ? __ldg(ts.tmask + sb + q) : 0ull;
-                int btot;
-                const int slot = block_excl_sum1<NT>(popc64(m), s_slot, btot) + run;
-                const long long key = v ? win_key_row(slot, q, t - tmin) : -1ll;
-                long long kmax;
-                const long long prev = block_excl_max1t<NT>(key, s_key, carry, kmax);
-                const bool start = v && key != prev;
-                int nst;
-                const int wpos = block_excl_sum1<NT>((int)start, s_st, nst) + wrun;
-                if (pass == 1) {
-                    if (start) {
-                        if (wpos < nwin) win[wbase + wpos] = Window{i, slot, 0, t, 0};
-                        else set_err(&ctl->err, DERR_INTERNAL);
-                    }
-                    // this thread's tile: lanes of a warp write their tiles' columns together
-                    // (every lane takes part in the step count; a tile past the row's end is
-                    // an internal error and writes nothing)
-                    const bool fits = slot + popc64(m) <= nnz;
-                    if (!fits) set_err(&ctl->err, DERR_INTERNAL);
-                    unsigned long long mm = fits ? m : 0ull;
-                    int *o = ccol + rowbase + slot;
-                    const int cb = t << 6;
-                    const int steps = (int)__reduce_max_sync(FULL, (unsigned)popc64(mm));
-                    for (int k = 0; k < steps; k++) {
-                        if (mm) {
-                            *o++ = cb + (__ffsll((long long)mm) - 1);
-                            mm &= mm - 1ull;
-                        }
-                    }
+                const long long info = v ? __ldg(ts.tinfo + sb + q) : 0ll;
+                const int slot = (int)(unsigned)info;
+                const int ord1 = (int)(info >> 32);
+                if (ord1) {
+                    if (ord1 <= nwin) win[wbase + ord1 - 1] = Window{i, slot, 0, t, 0};
+                    else set_err(&ctl->err, DERR_INTERNAL);
                 }
-                run += btot;
-                wrun += nst;
-                carry = kmax;
+                // the 32 tiles' entries: slots s0 .. s0 + (their entries) - 1 of the row
+                const int s0 = __shfl_sync(FULL, slot, 0);
+                const int total = warp_sum(popc64(m));
+                if (s0 + total <= nnz) warp_emit_list(t, m, ccol + rowbase + s0);
+                else if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
             }
-            if (pass == 0) {
-                if (threadIdx.x == 0) {
-                    int wb = -1;
-                    if (run != nnz) {
-                        set_err(&ctl->err, DERR_INTERNAL);
-                    } else if (wrun > 0) {
-                        wb = atomicAdd(&ctl->win_count, wrun);
-                        if ((long long)wb + wrun > win_cap) {
-                            set_err(&ctl->err, DERR_CAPACITY);
-                            wb = -1;
-                        }
-                    }
-                    s_wbase = wb;
-                }
-                __syncthreads();
-                wbase = s_wbase;
-                nwin = wrun;
-                if (wbase < 0) break;  // no windows, or an error already reported
-            }
+        } else if (threadIdx.x == 0) {
+            set_err(&ctl->err, DERR_CAPACITY);
         }
-        __syncthreads();  // the row's window starts, written by this block, are visible to it
-        if (wbase >= 0) {
-            // every window's slot count: the next window's first slot, or the row's end
-            for (int j = threadIdx.x; j < nwin; j += NT) {
-                const int s0 = win[wbase + j].s0;
-                const int e = j + 1 < nwin ? win[wbase + j + 1].s0 : nnz;
-                win[wbase + j].cnt = e - s0;
-            }
-        }
-        __syncthreads();  // s_wbase and the scan arrays are reused by the next row
+        if (!ts.wbase) __syncthreads();  // s_wbase is reused by the next row
     }
 }
 
@@ -551,11 +509,11 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
             A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
     }
     if (!class_rows || class_rows[BIN_L] > 0) {
-        if (ts && ts->tcol && out.mode == OUT_PLAIN)
-            k_struct_ls<<<nsm * 8, SLS_THREADS, 0, st>>>(A.M, ri, *ts, out, win, win_cap, ctl);
-        else
+        const bool store = ts && ts->cnt && out.mode == OUT_PLAIN;
+        if (store) k_struct_ls<<<nsm * 6, SLS_THREADS, 0, st>>>(A.M, ri, *ts, out, win, win_cap, ctl);
+        if (!store || !ts->all_stored)
             k_struct_l<<<nsm * 3, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
-                                                                    win, win_cap, ctl);
+                                                                    win, win_cap, store ? ts->cnt : nullptr, ctl);
     }
 }
 

@@ -22,6 +22,7 @@
 #include "hsmu_block.cuh"
 #include "hsmu_kernels.h"
 #include "hsmu_rowops.cuh"
+#include "hsmu_tilelist.cuh"
 
 namespace hsmu {
 
@@ -64,10 +65,9 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
 }
 
 constexpr int L_THREADS = 256;
-constexpr int L_PER = DCH_COUNT / L_THREADS;  // consecutive tiles per thread when storing
 
 template <bool STORE>
-__global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restrict__ arp,
+__global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__restrict__ arp,
                                                        const int *__restrict__ acol,
                                                        const int *__restrict__ tptr,
                                                        const int *__restrict__ tcol,
@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
     extern __shared__ unsigned long long s_dyn[];
     unsigned long long *msk = s_dyn;  // DCH_COUNT entries
     __shared__ int s_red[L_THREADS / 32];
-    __shared__ long long s_pk[L_THREADS / 32];
+    __shared__ ListSmem<L_THREADS / 32> s_ls;
+    __shared__ long long s_off;
     const int lane = lane_id(), w = threadIdx.x >> 5;
     constexpr int NWARP = L_THREADS / 32;
     const int n = ctl->bin_count[BIN_L];
@@ -86,9 +87,22 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
         const int a_lo = arp[i], a_hi = arp[i + 1];
         const bool one_chunk = (tmax - tmin + 1) <= DCH_COUNT;
-        int total = 0, stored = 0;
-        const long long sbase = STORE ? ts.off[i] : 0;
+        int total = 0;
+        ListRun run{0, 0, 0, -1ll};
+        long long sbase = -1;
         const int scap = STORE ? ri.tcap[i] : 0;
+        if (STORE) {
+            // reserve the row's list in the arena (none when it is full)
+            if (threadIdx.x == 0) {
+                long long o = atomicAdd(reinterpret_cast<unsigned long long *>(&ctl->store_used),
+                                        (unsigned long long)scap);
+                if (o + scap > ts.cap) o = -1;
+                s_off = o;
+                ts.off[i] = o;
+            }
+            __syncthreads();
+            sbase = s_off;
+        }
         for (int c0 = tmin; c0 <= tmax; c0 += DCH_COUNT) {
             const int c1 = min(c0 + DCH_COUNT, tmax + 1);
             for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) msk[t] = 0ull;
@@ -100,35 +114,14 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
                 warp_or_tiles<true, true>(a_lo, a_hi, w * WARP, NWARP * WARP, acol, tptr, tcol, tmask, c0, c1 - c0, msk, bad);
             if (bad) set_err(&ctl->err, DERR_INTERNAL);
             __syncthreads();
-            if (STORE) {
-                // each thread: L_PER consecutive tiles; one packed block scan gives the
-                // chunk's entries and every thread's place in the row's tile list
-                const int len = c1 - c0;
-                const int lo = min(len, (int)threadIdx.x * L_PER), hi = min(len, lo + L_PER);
-                int pc = 0, ne = 0;
-                for (int t = lo; t < hi; t++) {
-                    const unsigned long long m = msk[t];
-                    pc += popc64(m);
-                    ne += m != 0ull;
-                }
-                long long tot;
-                const long long ex = block_excl_sum1<L_THREADS>(((long long)pc << 32) | ne, s_pk, tot);
-                const int chunk_tiles = (int)(tot & 0xffffffffll);
-                if (stored + chunk_tiles > scap) {
-                    if (threadIdx.x == 0) set_err(&ctl->err, DERR_INTERNAL);
-                } else {
-                    long long pos = sbase + stored + (int)(ex & 0xffffffffll);
-                    for (int t = lo; t < hi; t++) {
-                        const unsigned long long m = msk[t];
-                        if (m) {
-                            ts.tcol[pos] = c0 + t;
-                            ts.tmask[pos] = m;
-                            pos++;
-                        }
-                    }
-                }
-                stored += chunk_tiles;
-                total += (int)(tot >> 32);
+            if (STORE && sbase >= 0) {
+                // the chunk's non-empty tiles appended to the row's list, with their slots
+                // and window starts (hsmu_tilelist.cuh)
+                if (!chunk_to_list<NWARP>(msk, c1 - c0, c0, tmin, run, s_ls, sbase, scap, ts.tcol, ts.tmask,
+                                          ts.tinfo) &&
+                    threadIdx.x == 0)
+                    set_err(&ctl->err, DERR_INTERNAL);
+                total = run.slots;
             } else {
                 int cnt = 0;
                 for (int t = threadIdx.x; t < c1 - c0; t += L_THREADS) cnt += popc64(msk[t]);
@@ -145,7 +138,13 @@ __global__ void __launch_bounds__(L_THREADS) k_count_l(int M, const int *__restr
         }
         if (threadIdx.x == 0) {
             ri.cnnz[i] = total;
-            if (STORE) ts.cnt[i] = min(stored, scap);  // over the capacity: reported above
+            if (STORE) {
+                ts.cnt[i] = sbase < 0 ? -1 : min(run.tiles, scap);  // over the capacity: reported above
+                ts.nwin[i] = run.wins;
+                // the row's windows, contiguous: their place is reserved now (the array
+                // itself is allocated after this pass, from the bound on windows)
+                if (ts.wbase) ts.wbase[i] = sbase < 0 ? -1 : atomicAdd(&ctl->win_count, run.wins);
+            }
         }
     }
 }
@@ -179,7 +178,7 @@ void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, Ro
 void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,
                         cudaStream_t st) {
     const size_t smem = DCH_COUNT * sizeof(unsigned long long);
-    if (ts && ts->tcol && ri.tcap)
+    if (ts && ts->tcol && ts->tinfo && ts->cap > 0 && ri.tcap)
         k_count_l<true><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, *ts, ctl);
     else
         k_count_l<false><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri,

@@ -25,9 +25,13 @@ HSMU_ERR_TIMEOUT = 7
 
 def pool_used_bytes():
     """bytes in use from the device's default stream-ordered memory pool
-    (what the library allocates from), after the device has finished"""
+    (what the library allocates from), after the device has finished and
+    unreferenced outputs of earlier tests have been released"""
+    import gc
+
     import hsmu_gb
 
+    gc.collect()
     hsmu_gb.load_library()
     rt = ctypes.CDLL("libcudart.so.13")
     assert rt.cudaDeviceSynchronize() == 0

@@ -120,7 +120,7 @@ def test_learned_identical_to_plain(engine, name):
     np.testing.assert_array_equal(C.col, P.col)
     assert np.array_equal(C.val.view(np.int64), P.val.view(np.int64))
     assert st["nnz_c"] == P.nnz
-    if st["spec_capacity"] < P.nnz:  # only possible when some rows overflowed their slots
+    if not st["routed"] and st["spec_capacity"] < P.nnz:  # only when some rows overflowed their slots
         assert st["fallback_rows"] > 0
 
 
@@ -142,8 +142,9 @@ def test_learned_fma_mode(engine):
 def test_learned_all_rows_fall_back(engine):
     # a model that predicts nothing fits: every non-tiny row is redone, result unchanged
     p, _ = model_for_tests(engine)
-    A = gen.rmat(12, 16, seed=4, lo=-1.0, hi=1.0)
+    A = gen.rmat(16, 8, seed=4, lo=-1.0, hi=1.0)  # has rows of the large class: not handed to the plain path
     P, C, st = run_both(engine, A, A, p, -40.0)
+    assert not st["routed"]
     assert st["fallback_rows"] > 0
     np.testing.assert_array_equal(C.col, P.col)
     assert np.array_equal(C.val.view(np.int64), P.val.view(np.int64))
@@ -159,3 +160,16 @@ def test_trained_model_sizes_slots_tighter_than_the_bound(engine):
     prods = gen.products(A, A)
     assert st["spec_capacity"] < 0.25 * prods           # the bound would allocate `prods` entries
     assert st["fallback_rows"] <= 0.15 * A.M            # boundary rows of a small grid are the hardest
+
+
+@pytest.mark.parametrize("name", ["lap", "st27"])
+def test_inputs_without_windowed_rows_go_to_the_plain_path(engine, name):
+    # every row tiny (Laplacian), or no large row and none predicted above the fused
+    # warp path (stencil): the plain path finishes the product on the same tiles
+    p, margin = model_for_tests(engine)
+    A = gen.laplacian2d(96, seed=0) if name == "lap" else gen.stencil27(12, 3, seed=1)
+    P, C, st = run_both(engine, A, A, p, margin)
+    assert st["routed"] == 1
+    np.testing.assert_array_equal(C.row_ptr, P.row_ptr)
+    np.testing.assert_array_equal(C.col, P.col)
+    assert np.array_equal(C.val.view(np.int64), P.val.view(np.int64))
