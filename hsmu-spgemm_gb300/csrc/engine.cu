@@ -694,7 +694,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     }
     PlainRun r(h, st, o);
     rc = r.begin(A, B);
-    if (!rc) rc = r.tiles_bounds(B, nullptr, stats != nullptr, stats ? h->ev[1] : nullptr, false);
+    if (!rc) rc = r.tiles_bounds(B, nullptr, stats != nullptr, stats ? h->ev[1] : nullptr, o.no_tile_store == 0);
     if (rc) goto done;
     CK(cudaMemcpyAsync(h->h_ctl, r.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -705,11 +705,25 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
     }
     if (hc.bin_count[BIN_L] == 0 && hc.bin_count[BIN_DS] == 0) goto plain;
     {
+        // the large rows' tile lists: the arena is sized now, from the bounds pass's need
+        if (r.ri.tcap && hc.bin_count[BIN_L] > 0) {
+            if (hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;
+            CK(r.grow_arena());
+            if (h->arena_cap > 0 && !r.ts_off) {
+                CK(palloc(&r.ts_off, (size_t)M, st));
+                CK(palloc(&r.ts_cnt, (size_t)M, st));
+                CK(palloc(&r.ts_nwin, (size_t)M, st));
+                CK(palloc(&r.ts_wbase, (size_t)M, st));
+            }
+            r.have_store = h->arena_cap > 0;
+        }
         CK(palloc(&feat, (size_t)M, st));
         CK(palloc(&cap, (size_t)M + 1, st));
         CK(palloc(&soff, (size_t)M + 1, st));
         launch_features(r.Ad, r.Bd, feat, nullptr, h->nsm, st);
-        launch_capacity(model->params, feat, r.ri.prod, M, B->N, model->margin, cap, h->nsm, st, &r.ctl->pred_wide);
+        // large rows with a tile list need no slot (they are written at their place in C)
+        launch_capacity(model->params, feat, r.ri.prod, M, B->N, model->margin, cap, h->nsm, st, &r.ctl->pred_wide,
+                        r.have_store ? r.ri.cls : nullptr);
         launch_scan64(cap, soff, M, &r.ctl->nnz, r.scan_tmp, st);  // nnz field holds the slot total for now
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(h->h_ctl, r.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -784,9 +798,23 @@ learned:
             CK(palloc(&wc.cur, (size_t)cur_cap, st));
         }
         if (stats) cudaEventRecord(h->ev[3], st);
-        // structure (+ values of warp-sized rows) into the slots; exact counts found here
-        launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M}, win,
-                         win_cap, ctl, o.arith, h->nsm, st);
+        // structure (+ values of warp-sized rows) into the slots; exact counts found here.
+        // Large rows with a tile list: exact count and list now, written at their place in
+        // C by the redo pass (the prediction has nothing to skip for them: their count pass
+        // builds the list the structure pass streams).
+        const RowOut spec{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M};
+        // listed large rows reserve their windows in the speculative count pass (the window
+        // array exists by then), so the redo pass streams them without barriers
+        TileStore tsd{r.ts_off, r.ts_cnt, r.ts_nwin, r.ts_wbase, h->arena_col, h->arena_mask, h->arena_info,
+                      h->arena_cap, 0};
+        const int small_rows[NBIN] = {hc.bin_count[BIN_DS], 0, hc.bin_count[BIN_TINY]};
+        const int large_rows[NBIN] = {0, hc.bin_count[BIN_L], 0};
+        launch_structure(Ad, Bd, Btd, ri, spec, win, win_cap, ctl, o.arith, h->nsm, st, small_rows);
+        if (hc.bin_count[BIN_L] > 0) {
+            if (r.have_store) launch_spec_large(Ad, Btd, ri, tsd, spec, ctl, h->nsm, st);
+            launch_structure(Ad, Bd, Btd, ri, spec, win, win_cap, ctl, o.arith, h->nsm, st, large_rows,
+                             r.have_store ? &tsd : nullptr);
+        }
         launch_scan(ri.cnnz, crp, M, &ctl->nnz, r.scan_tmp, ctl, st);
         // exact nnz(C): rows that overflowed their slot can make it larger than the slot total
         CK(cudaGetLastError());
@@ -805,7 +833,7 @@ learned:
         CK(palloc(&cval, (size_t)hc.nnz, st));
         launch_compact(M, soff, crp, flag, scol, sval, ccol, cval, h->nsm, st);
         launch_structure(Ad, Bd, Btd, ri, RowOut{OUT_REDO, crp, nullptr, ccol, cval, nullptr, flag, 0, M}, win,
-                         win_cap, ctl, o.arith, h->nsm, st);
+                         win_cap, ctl, o.arith, h->nsm, st, nullptr, r.have_store ? &tsd : nullptr);
         if (stats) cudaEventRecord(h->ev[4], st);
         launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, flag, scol, soff, wc, ctl, o.arith, h->nsm, st,
                        o.wait_polls);

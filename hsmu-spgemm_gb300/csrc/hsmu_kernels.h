@@ -93,9 +93,10 @@ void launch_scan64(const int *in, long long *out, int n, long long *total64, int
 
 // learned.cu
 void launch_features(const DevCSR &A, const DevCSR &B, float4 *feat, long long *prod_out, int nsm, cudaStream_t st);
-// wide (nullable): incremented for every row whose slot exceeds FUSE_CAP entries
+// wide (nullable): incremented for every row predicted clearly above FUSE_CAP entries;
+// cls (nullable): rows of the large class get no slot (the caller keeps their tile lists)
 void launch_capacity(const float *params, const float4 *feat, const long long *prod, int M, int N, float margin,
-                     int *cap, int nsm, cudaStream_t st, int *wide = nullptr);
+                     int *cap, int nsm, cudaStream_t st, int *wide = nullptr, const signed char *cls = nullptr);
 void launch_compact(int M, const long long *soff, const int *crp, const unsigned char *flag, const int *scol,
                     const double *sval, int *ccol, double *cval, int nsm, cudaStream_t st);
 
@@ -108,6 +109,11 @@ void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, Ro
                         cudaStream_t st);
 void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,
                         cudaStream_t st);
+// learned path, large rows: exact count and tile list in its speculative pass;
+// every listed row is flagged ROW_OVERFLOW (out.flag) so that the pass after the
+// exact scan writes it at its place in C (k_symbolic.cu)
+void launch_spec_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore &ts, RowOut out, Ctl *ctl,
+                       int nsm, cudaStream_t st);
 
 // k_structure.cu
 // writes C's columns and numeric windows; rows that fit one warp also get their values

@@ -67,13 +67,18 @@ static_assert(WIN_CAP * 8 >= (WIN_CAP + 8) * 4, "column stage fits in the accumu
 // count of 0 (the large rows built from their stored tiles) gets its count
 // here: up to the next window's first slot when that window continues the
 // same row, else up to the row's end.
-__global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int win_cap, const int *__restrict__ arp,
-                                                 const int *__restrict__ crp, const Ctl *ctl, int *__restrict__ len) {
+__global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int win_cap, int M, const int *__restrict__ arp,
+                                                 const int *__restrict__ crp, Ctl *ctl, int *__restrict__ len) {
     const int nwin = min(ctl->win_count, win_cap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < win_cap; w += gridDim.x * blockDim.x) {
         int n = 0;
         if (w < nwin) {
             const int row = win[w].row;
+            if ((unsigned)row >= (unsigned)M) {  // a window left unwritten after a reported error
+                set_err(&ctl->err, DERR_INTERNAL);
+                len[w] = 0;
+                continue;
+            }
             n = arp[row + 1] - arp[row];
             if (win[w].cnt == 0) {
                 const int s0 = win[w].s0;
@@ -94,7 +99,7 @@ __global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int w
 // one binary search and then forward gallops per A entry -- was measured
 // slower: R-MAT 18 value stage 28.1 -> 30.4 ms, the chained gallops of a heavy
 // row's group form a tail and fewer searches run at once.)
-__global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ win, int win_cap,
+__global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ win, int win_cap, int M,
                                                      const long long *__restrict__ woff, long long cur_cap,
                                                      const int *__restrict__ arp, const int *__restrict__ acol,
                                                      const int *__restrict__ brp, const int *__restrict__ tptr,
@@ -106,6 +111,7 @@ __global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ 
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int w = gw; w < nwin; w += nw) {
         const Window W = win[w];
+        if ((unsigned)W.row >= (unsigned)M) continue;  // reported by k_win_len
         const int a_lo = arp[W.row], a_hi = arp[W.row + 1];
         const long long base = woff[w];
         if (base + (a_hi - a_lo) > cur_cap) {
@@ -134,7 +140,7 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             const int *__restrict__ scol,
                                                             const long long *__restrict__ soff,
                                                             const long long *__restrict__ woff,
-                                                            const int *__restrict__ wcur, int wait_polls,
+                                                            const int *__restrict__ wcur, int wait_polls, int M,
                                                             Ctl *ctl) {
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
@@ -156,6 +162,10 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
         for (int wi = g * GW; wi < wend; wi++) {
             const Window W = win[wi];
             const int row = W.row, cnt = W.cnt, t0 = W.t0;
+            if ((unsigned)row >= (unsigned)M) {  // reported by k_win_len
+                bad = true;
+                continue;
+            }
             if (flag && flag[row] == ROW_OVERFLOW && !W.redo) continue;  // stale: the redo pass emitted fresh windows
             const int row_lo = crp[row], row_hi = crp[row + 1];
             const int s0 = row_lo + W.s0;  // windows carry row-relative offsets
@@ -332,14 +342,14 @@ void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const 
                     int wait_polls) {
     if (win_cap <= 0) return;
     cudaMemsetAsync(&ctl->win_next, 0, sizeof(int), st);
-    k_win_len<<<nsm * 4, 256, 0, st>>>(const_cast<Window *>(win), (int)win_cap, A.rp, crp, ctl, wc.len);
+    k_win_len<<<nsm * 4, 256, 0, st>>>(const_cast<Window *>(win), (int)win_cap, A.M, A.rp, crp, ctl, wc.len);
     launch_scan64(wc.len, wc.off, (int)win_cap, wc.total, wc.scan_tmp, st);
-    k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
+    k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, A.M, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
                                             Bt.off, wc.cur, ctl);
     auto k = arith == AR_IMUL ? k_numeric<AR_IMUL> : arith == AR_FMA ? k_numeric<AR_FMA> : k_numeric<AR_RN>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
         A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, wc.off, wc.cur,
-        wait_polls, ctl);
+        wait_polls, A.M, ctl);
 }
 
 int configure_numeric() {

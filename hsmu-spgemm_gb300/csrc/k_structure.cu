@@ -265,7 +265,8 @@ struct SlSmem {
 };
 
 // stored: nullable per-row tile-list counts of the tile store; rows that have a
-// list (>= 0) are built by k_struct_ls and skipped here
+// list (>= 0) are built by k_struct_ls (or, learned path, by the count kernel)
+// and skipped here
 __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__restrict__ arp,
                                                          const int *__restrict__ acol,
                                                          const int *__restrict__ tptr,
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(SLS_THREADS, 6) k_struct_ls(int M, RowInfo ri,
         if (n < 0) continue;  // no list kept (the arena was full): k_struct_l builds this row
         const long long sb = ts.off[i];
         const int nwin = ts.nwin[i];
-        const long long rowbase = out.crp[i];
+        const long long rowbase = out.crp[i];  // PLAIN or REDO: final row pointers
         const int nnz = out.crp[i + 1] - out.crp[i];
         int wbase;
         if (ts.wbase) {
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(SLS_THREADS, 6) k_struct_ls(int M, RowInfo ri,
                 const int slot = (int)(unsigned)info;
                 const int ord1 = (int)(info >> 32);
                 if (ord1) {
-                    if (ord1 <= nwin) win[wbase + ord1 - 1] = Window{i, slot, 0, t, 0};
+                    if (ord1 <= nwin) win[wbase + ord1 - 1] = Window{i, slot, 0, t, out.mode == OUT_REDO};
                     else set_err(&ctl->err, DERR_INTERNAL);
                 }
                 // the 32 tiles' entries: slots s0 .. s0 + (their entries) - 1 of the row
@@ -509,11 +510,13 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
             A.M, A.rp, A.col, A.val, B.rp, B.col, B.val, Bt.ptr, Bt.col, Bt.mask, ri, out, win, win_cap, ctl);
     }
     if (!class_rows || class_rows[BIN_L] > 0) {
-        const bool store = ts && ts->cnt && out.mode == OUT_PLAIN;
-        if (store) k_struct_ls<<<nsm * 6, SLS_THREADS, 0, st>>>(A.M, ri, *ts, out, win, win_cap, ctl);
-        if (!store || !ts->all_stored)
+        // rows with a stored tile list are streamed by k_struct_ls (PLAIN, REDO; in SPEC
+        // mode the count kernel already wrote them), the others take the OR walk
+        const bool list = ts && ts->cnt;
+        if (list && out.mode != OUT_SPEC) k_struct_ls<<<nsm * 6, SLS_THREADS, 0, st>>>(A.M, ri, *ts, out, win, win_cap, ctl);
+        if (!list || !ts->all_stored)
             k_struct_l<<<nsm * 3, SL_THREADS, sizeof(SlSmem), st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, out,
-                                                                    win, win_cap, store ? ts->cnt : nullptr, ctl);
+                                                                    win, win_cap, list ? ts->cnt : nullptr, ctl);
     }
 }
 

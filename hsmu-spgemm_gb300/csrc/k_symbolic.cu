@@ -66,13 +66,31 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
 
 constexpr int L_THREADS = 256;
 
-template <bool STORE>
+// Large rows, one CTA per row: the OR of B's tile masks per chunk of the row's
+// tile span, then
+//   LM_COUNT  the row's nnz;
+//   LM_STORE  also the row's tile list in the arena (the plain path: the
+//             structure pass streams it once C is allocated);
+//   LM_SPEC   the same in the learned path's speculative pass: the row is
+//             flagged ROW_OVERFLOW so that the pass after the exact scan
+//             writes it, from its list, straight to its place in C.  (Writing
+//             the columns into the predicted slot in this pass, so that the
+//             list needs no second pass, was measured slower: R-MAT 18 47.3 ms
+//             against 44.1 for the plain path -- the emission lengthens this
+//             barrier-bound kernel, and the slot still has to be copied to C.)
+// A row that finds the arena full keeps no list (ts.cnt = -1) and is left to
+// the OR-walk structure kernel.
+enum LMode { LM_COUNT = 0, LM_STORE = 1, LM_SPEC = 2 };
+
+template <int MODE>
 __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__restrict__ arp,
                                                        const int *__restrict__ acol,
                                                        const int *__restrict__ tptr,
                                                        const int *__restrict__ tcol,
                                                        const unsigned long long *__restrict__ tmask,
-                                                       RowInfo ri, TileStore ts, Ctl *ctl) {
+                                                       RowInfo ri, TileStore ts, RowOut out, Ctl *ctl) {
+    constexpr bool STORE = MODE != LM_COUNT;
+    constexpr bool SPEC = MODE == LM_SPEC;
     extern __shared__ unsigned long long s_dyn[];
     unsigned long long *msk = s_dyn;  // DCH_COUNT entries
     __shared__ int s_red[L_THREADS / 32];
@@ -136,15 +154,17 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
             }
             __syncthreads();
         }
+        const bool listed = STORE && sbase >= 0 && run.tiles <= scap;
         if (threadIdx.x == 0) {
             ri.cnnz[i] = total;
             if (STORE) {
-                ts.cnt[i] = sbase < 0 ? -1 : min(run.tiles, scap);  // over the capacity: reported above
+                ts.cnt[i] = listed ? run.tiles : -1;  // over the capacity: reported above
                 ts.nwin[i] = run.wins;
                 // the row's windows, contiguous: their place is reserved now (the array
                 // itself is allocated after this pass, from the bound on windows)
-                if (ts.wbase) ts.wbase[i] = sbase < 0 ? -1 : atomicAdd(&ctl->win_count, run.wins);
+                if (ts.wbase) ts.wbase[i] = listed ? atomicAdd(&ctl->win_count, run.wins) : -1;
             }
+            if (SPEC) out.flag[i] = listed ? ROW_OVERFLOW : ROW_NONE;  // unlisted: the OR-walk kernel
         }
     }
 }
@@ -179,10 +199,17 @@ void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const T
                         cudaStream_t st) {
     const size_t smem = DCH_COUNT * sizeof(unsigned long long);
     if (ts && ts->tcol && ts->tinfo && ts->cap > 0 && ri.tcap)
-        k_count_l<true><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, *ts, ctl);
+        k_count_l<LM_STORE><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, *ts,
+                                                               RowOut{}, ctl);
     else
-        k_count_l<false><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri,
-                                                           TileStore{}, ctl);
+        k_count_l<LM_COUNT><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri,
+                                                               TileStore{}, RowOut{}, ctl);
+}
+
+void launch_spec_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore &ts, RowOut out, Ctl *ctl,
+                       int nsm, cudaStream_t st) {
+    const size_t smem = DCH_COUNT * sizeof(unsigned long long);
+    k_count_l<LM_SPEC><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, ts, out, ctl);
 }
 
 void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int nsm,
@@ -192,7 +219,7 @@ void launch_count(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo 
 }
 
 int configure_count() {
-    for (auto k : {k_count_l<false>, k_count_l<true>}) {
+    for (auto k : {k_count_l<LM_COUNT>, k_count_l<LM_STORE>, k_count_l<LM_SPEC>}) {
         const int e = (int)cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 DCH_COUNT * (int)sizeof(unsigned long long));
         if (e) return e;

@@ -241,7 +241,8 @@ __global__ void k_adam(float *__restrict__ params, const float *__restrict__ gra
 // always fit), min(products, N, 2^(prediction + margin)) otherwise.
 __global__ void __launch_bounds__(256) k_capacity(const float *__restrict__ params, const float4 *__restrict__ feat,
                                                   const long long *__restrict__ prod, int M, int N, float margin,
-                                                  int *__restrict__ cap, int *wide) {
+                                                  int *__restrict__ cap, int *wide,
+                                                  const signed char *__restrict__ cls) {
     __shared__ float P[MLP_NTOTAL];
     for (int q = threadIdx.x; q < MLP_NTOTAL; q += blockDim.x) P[q] = params[q];
     __syncthreads();
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(256) k_capacity(const float *__restrict__ para
         const long long pr = prod[i];
         const long long bound = pr < (long long)N ? pr : (long long)N;
         long long c = bound;
-        bool w = false;  // predicted (without the slot margin) wider than the fused warp path
+        bool w = false;  // predicted clearly wider than the fused warp path (routing only)
         if (pr > TINY_MAX) {
             float h1[H], h2[H];
             const float y = mlp_eval(P, feat[i], h1, h2, nullptr, nullptr) * P[OFF_YSD] + P[OFF_YMU];
@@ -257,8 +258,9 @@ __global__ void __launch_bounds__(256) k_capacity(const float *__restrict__ para
             const long long pc = (long long)ceilf(exp2f(fmaxf(e, 0.f)));
             c = pc < bound ? pc : bound;
             if (c < 1) c = 1;
-            w = y > log2f((float)FUSE_CAP) && bound > FUSE_CAP;
+            w = y > log2f((float)FUSE_CAP) + 0.5f && bound > FUSE_CAP;  // half a step of slack
         }
+        if (cls && cls[i] == BIN_L) c = 0;  // a large row with a tile list takes no slot
         cap[i] = (int)c;
         // such rows go through numeric windows
         if (wide) {
@@ -289,8 +291,8 @@ __global__ void __launch_bounds__(256) k_compact(int M, const long long *__restr
 }
 
 void launch_capacity(const float *params, const float4 *feat, const long long *prod, int M, int N, float margin,
-                     int *cap, int nsm, cudaStream_t st, int *wide) {
-    k_capacity<<<nsm * 4, 256, 0, st>>>(params, feat, prod, M, N, margin, cap, wide);
+                     int *cap, int nsm, cudaStream_t st, int *wide, const signed char *cls) {
+    k_capacity<<<nsm * 4, 256, 0, st>>>(params, feat, prod, M, N, margin, cap, wide, cls);
 }
 
 void launch_compact(int M, const long long *soff, const int *crp, const unsigned char *flag, const int *scol,
