@@ -299,7 +299,8 @@ struct PlainRun {
                 CKR(palloc(&ts_off, (size_t)M, st));
                 CKR(palloc(&ts_cnt, (size_t)M, st));
                 CKR(palloc(&ts_nwin, (size_t)M, st));
-                if (reserve_windows) CKR(palloc(&ts_wbase, (size_t)M, st));
+                CKR(cudaMemsetAsync(ts_nwin, 0, sizeof(int) * (size_t)M, st));
+                if (reserve_windows) CKR(palloc(&ts_wbase, (size_t)M + 1, st));
                 have_store = true;
             }
         }
@@ -337,6 +338,13 @@ struct PlainRun {
         launch_count_small(Ad, Bd, Btd, ri, ctl, h->nsm, st);
         const TileStore tsd = store_view();
         launch_count_large(Ad, Btd, ri, have_store ? &tsd : nullptr, ctl, h->nsm, st);
+        if (have_store && ts_wbase) {
+            // the listed rows' windows in row order, ahead of every other window: the value
+            // pass hands windows out in array order, and R-MAT's heaviest rows come first
+            launch_scan(ts_nwin, ts_wbase, M, &ctl->win_listed, scan_tmp, ctl, st);
+            CKR(cudaMemcpyAsync(&ctl->win_count, ts_wbase + M, sizeof(int), cudaMemcpyDeviceToDevice, st));
+            launches += 3;
+        }
         launch_scan(ri.cnnz, crp, M, &ctl->nnz, scan_tmp, ctl, st);
         launches += 6;  // count 3, scan 3
         CKR(cudaGetLastError());
@@ -713,7 +721,8 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
                 CK(palloc(&r.ts_off, (size_t)M, st));
                 CK(palloc(&r.ts_cnt, (size_t)M, st));
                 CK(palloc(&r.ts_nwin, (size_t)M, st));
-                CK(palloc(&r.ts_wbase, (size_t)M, st));
+                CK(cudaMemsetAsync(r.ts_nwin, 0, sizeof(int) * (size_t)M, st));
+                CK(palloc(&r.ts_wbase, (size_t)M + 1, st));
             }
             r.have_store = h->arena_cap > 0;
         }
@@ -803,18 +812,23 @@ learned:
         // C by the redo pass (the prediction has nothing to skip for them: their count pass
         // builds the list the structure pass streams).
         const RowOut spec{OUT_SPEC, nullptr, soff, scol, sval, ri.cnnz, flag, 0, M};
-        // listed large rows reserve their windows in the speculative count pass (the window
-        // array exists by then), so the redo pass streams them without barriers
+        // The listed large rows' windows are placed first, in row order (scan of their
+        // counts), before any warp row's window: the value pass hands windows out in array
+        // order, and R-MAT's heaviest rows come first.  The redo pass then streams those rows
+        // without barriers.
         TileStore tsd{r.ts_off, r.ts_cnt, r.ts_nwin, r.ts_wbase, h->arena_col, h->arena_mask, h->arena_info,
                       h->arena_cap, 0};
         const int small_rows[NBIN] = {hc.bin_count[BIN_DS], 0, hc.bin_count[BIN_TINY]};
         const int large_rows[NBIN] = {0, hc.bin_count[BIN_L], 0};
+        if (hc.bin_count[BIN_L] > 0 && r.have_store) {
+            launch_spec_large(Ad, Btd, ri, tsd, spec, ctl, h->nsm, st);
+            launch_scan(r.ts_nwin, r.ts_wbase, M, &ctl->win_listed, r.scan_tmp, ctl, st);
+            CK(cudaMemcpyAsync(&ctl->win_count, r.ts_wbase + M, sizeof(int), cudaMemcpyDeviceToDevice, st));
+        }
         launch_structure(Ad, Bd, Btd, ri, spec, win, win_cap, ctl, o.arith, h->nsm, st, small_rows);
-        if (hc.bin_count[BIN_L] > 0) {
-            if (r.have_store) launch_spec_large(Ad, Btd, ri, tsd, spec, ctl, h->nsm, st);
+        if (hc.bin_count[BIN_L] > 0)
             launch_structure(Ad, Bd, Btd, ri, spec, win, win_cap, ctl, o.arith, h->nsm, st, large_rows,
                              r.have_store ? &tsd : nullptr);
-        }
         launch_scan(ri.cnnz, crp, M, &ctl->nnz, r.scan_tmp, ctl, st);
         // exact nnz(C): rows that overflowed their slot can make it larger than the slot total
         CK(cudaGetLastError());

@@ -85,6 +85,7 @@ struct Ctl {
     long long store_tiles;           // sum of RowInfo::tcap: arena entries the large rows could use
     long long store_used;            // arena entries reserved by the count pass
     int pred_wide;                   // learned path: rows predicted above FUSE_CAP entries
+    long long win_listed;            // windows of the rows with a tile list (scan total)
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

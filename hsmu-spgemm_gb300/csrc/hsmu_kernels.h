@@ -62,8 +62,9 @@ struct RowInfo {
 struct TileStore {
     long long *off;             // [M] written by the count pass
     int *cnt;                   // [M] tiles stored per row, -1: none
-    int *nwin;                  // [M] numeric windows of the row (rows with a list)
-    int *wbase;                 // [M] index of the row's first window (reserved by the count pass)
+    int *nwin;                  // [M] numeric windows of the row (0 for rows without a list)
+    int *wbase;                 // [M+1] index of the row's first window: exclusive scan of nwin in row
+                                // order (nullable: the structure pass reserves them itself)
     int *tcol;                  // arena: tile ids
     unsigned long long *tmask;  // arena: column masks
     long long *tinfo;           // arena: first slot | (window ordinal + 1) << 32 (hsmu_tilelist.cuh)

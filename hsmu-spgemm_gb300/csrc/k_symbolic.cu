@@ -159,10 +159,7 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
             ri.cnnz[i] = total;
             if (STORE) {
                 ts.cnt[i] = listed ? run.tiles : -1;  // over the capacity: reported above
-                ts.nwin[i] = run.wins;
-                // the row's windows, contiguous: their place is reserved now (the array
-                // itself is allocated after this pass, from the bound on windows)
-                if (ts.wbase) ts.wbase[i] = listed ? atomicAdd(&ctl->win_count, run.wins) : -1;
+                ts.nwin[i] = listed ? run.wins : 0;   // scanned in row order into the rows' first windows
             }
             if (SPEC) out.flag[i] = listed ? ROW_OVERFLOW : ROW_NONE;  // unlisted: the OR-walk kernel
         }
