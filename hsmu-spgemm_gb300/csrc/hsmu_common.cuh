@@ -30,7 +30,7 @@ constexpr int SPAN_T = 512;
 // WIN_SPAN bits + WIN_TCAP rank-ordered masks) and accumulator fit one warp.
 constexpr int WIN_CAP = 1024;
 constexpr int WIN_CUT = WIN_CAP - 64;
-constexpr int WIN_TCAP = 512;
+constexpr int WIN_TCAP = 256;
 constexpr int WIN_SPAN = 4096;
 constexpr int WIN_OCCW = WIN_SPAN / 64;
 // Tiles per chunk of the CTA (large-row) kernels.

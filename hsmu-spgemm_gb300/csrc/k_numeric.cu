@@ -43,7 +43,7 @@
 namespace hsmu {
 
 constexpr int NUM_WARPS = 3;
-constexpr int NUM_CTAS_PER_SM = 5;
+constexpr int NUM_CTAS_PER_SM = 6;
 constexpr int GW = 2;  // consecutive windows per work item, handed out dynamically
 constexpr int STAGE_LIMIT = 1 << 20;  // polls of a column copy before the kernel reports a timeout
 

@@ -95,8 +95,8 @@ __device__ __forceinline__ int out_limit(const RowOut &o, int i) {
 
 constexpr int SDS_WARPS = 4;
 constexpr int SDS_CTAS_PER_SM = 6;
-constexpr int SDS_WL = 64;     // > max windows of one DS row (SPAN_T*64/WIN_CUT + 1)
-static_assert(SPAN_T * 64 / WIN_CUT + 1 < SDS_WL, "window list of a warp row");
+constexpr int SDS_WL = 64;     // > max windows of one DS row (slot cuts + tile cuts + 1)
+static_assert(SPAN_T * 64 / WIN_CUT + SPAN_T / WIN_TCAP + 1 < SDS_WL, "window list of a warp row");
 
 struct SdsSmem {
     unsigned long long msk[SPAN_T];
@@ -167,13 +167,16 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             __syncwarp();
             continue;
         }
+        // window key of a tile: its first slot's WIN_CUT block and its WIN_TCAP block of
+        // the row's span (a window then has < WIN_CAP slots and spans <= WIN_TCAP tiles)
+        auto wkey = [](int base, int t) { return ((base / WIN_CUT) << 8) | (t / WIN_TCAP); };
         int run = incl - sum;
         int lastkey = -1;
         for (int t = lo; t < hi; t++) {
             const unsigned long long m = S.msk[t];
             S.base[t] = (unsigned short)run;
             if (m) {
-                lastkey = run / WIN_CUT;
+                lastkey = wkey(run, t);
                 run += popc64(m);
             }
         }
@@ -207,7 +210,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             int kk = carry;
             for (int t = lo; t < hi; t++)
                 if (S.msk[t]) {
-                    const int key = S.base[t] / WIN_CUT;
+                    const int key = wkey(S.base[t], t);
                     if (key != kk) nst++;
                     kk = key;
                 }
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             int pos = st_incl - nst, kk = carry;
             for (int t = lo; t < hi; t++)
                 if (S.msk[t]) {
-                    const int key = S.base[t] / WIN_CUT;
+                    const int key = wkey(S.base[t], t);
                     if (key != kk) {
                         S.wl[pos] = S.base[t];
                         S.wt[pos] = (unsigned short)t;

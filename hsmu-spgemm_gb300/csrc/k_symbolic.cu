@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_count_ds(int M, const int *__
             ri.cnnz[i] = cnt;
             if (cnt > FUSE_CAP) {  // goes through numeric windows: count them for the cursor array
                 atomicAdd(&ctl->wide_rows, 1);
-                const unsigned long long wb = cnt / WIN_CUT + 1;
+                const unsigned long long wb = cnt / WIN_CUT + (span - 1) / WIN_TCAP + 1;
                 atomicAdd(&ctl->cur_bound, wb * (unsigned long long)(arp[i + 1] - arp[i]));
             }
         }
