@@ -10,8 +10,8 @@
 //
 // The same pass cuts every row into numeric windows: consecutive tiles whose
 // first slot lies in the same WIN_CUT-slot block and whose tile ids lie in the
-// same SPAN_T-tile block.  A window therefore holds < WIN_CAP slots and spans
-// <= SPAN_T tiles, which bounds the numeric kernel's shared memory, and long
+// same WIN_TCAP-tile block.  A window therefore holds < WIN_CAP slots and spans
+// <= WIN_TCAP tiles, which bounds the numeric kernel's shared memory, and long
 // rows are split across many warps and SMs (the reference sends rows with
 // more than 4096 nnz to one CTA of the spECK dense accumulator,
 // src/compressed/compressed_Cval.cuh:300-365).
