@@ -43,8 +43,8 @@ __device__ __forceinline__ void warp_walk_tiles(int a_lo, int a_hi, int first, i
             lo = ldx<NC>(tptr + k);
             hi = ldx<NC>(tend + k);
             if (RESTRICT) {
-                lo = lower_bound_i32(tcol, lo, hi, c0);
-                hi = lower_bound_i32(tcol, lo, hi, c1);
+                lo = lower_bound_x<NC>(tcol, lo, hi, c0);
+                hi = lower_bound_x<NC>(tcol, lo, hi, c1);
             }
         }
         const int len = hi - lo;

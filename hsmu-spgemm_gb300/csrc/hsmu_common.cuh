@@ -160,6 +160,16 @@ __device__ __forceinline__ int lower_bound_i32(const int *__restrict__ a, int lo
     return lo;
 }
 
+// the same, loading as ldx<NC> (for arrays written earlier in the same launch)
+template <bool NC>
+__device__ __forceinline__ int lower_bound_x(const int *a, int lo, int hi, int key) {
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (ldx<NC>(a + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
 // first index in [lo, hi) with a[idx] > key, searching forward from lo by
 // doubling steps (cheap when the answer is close to lo)
 __device__ __forceinline__ int gallop_gt(const int *__restrict__ a, int lo, int hi, int key) {

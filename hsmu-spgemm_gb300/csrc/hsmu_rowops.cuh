@@ -14,9 +14,8 @@
 // The per-thread lists live in shared memory laid out element-major
 // ([TINY_MAX][threads]) so that neighbouring threads hit neighbouring banks.
 //
-// B's row k is given as entries brp[k] .. bre[k]-1: bre = brp + 1 for a CSR
-// row pointer; the batched engine's intermediate rows (A*P of a Galerkin
-// product) sit in padded slots and have their own end array.
+// B's row k is given as entries brp[k] .. bre[k]-1 (bre = brp + 1 for a CSR
+// row pointer).
 #pragma once
 #include "hsmu_products.cuh"
 
@@ -65,23 +64,6 @@ struct TinyFetch {
     }
 };
 
-// intermediate products of row (a_lo..a_hi), counted until they pass `limit`,
-// TINY_BATCH A entries per round of independent loads
-template <bool NC = true>
-__device__ __forceinline__ int tiny_products(int a_lo, int a_hi, const int *__restrict__ acol,
-                                             const int *__restrict__ brp, const int *__restrict__ bre, int limit) {
-    int prod = 0;
-    for (int p0 = a_lo; p0 < a_hi && prod <= limit; p0 += TINY_BATCH) {
-        int k[TINY_BATCH];
-#pragma unroll
-        for (int u = 0; u < TINY_BATCH; u++) k[u] = p0 + u < a_hi ? ldx<NC>(acol + p0 + u) : -1;
-#pragma unroll
-        for (int u = 0; u < TINY_BATCH; u++)
-            if (k[u] >= 0) prod += ldx<NC>(bre + k[u]) - ldx<NC>(brp + k[u]);
-    }
-    return prod;
-}
-
 // number of distinct columns of row (a_lo..a_hi) of A*B; -1 if the row has
 // more than TINY_MAX products (caller classified it wrongly).
 template <bool NC = true>
@@ -109,16 +91,16 @@ __device__ __forceinline__ int tiny_row_count(int a_lo, int a_hi, const int *__r
     return n;
 }
 
-// Fills the row's sorted columns and values at out_col/out_val and returns
-// its nnz; returns -1 on an inconsistency (more than TINY_MAX products, or
-// more than `cap` distinct columns).
+// Builds the row's sorted distinct columns and their accumulated values in
+// the thread's list (cols/acc, element stride `stride`, TINY_MAX entries) and
+// returns its length; returns -1 (list contents undefined) when the row has
+// more than `limit` products (limit <= TINY_MAX).
 template <int AR, bool NC = true>
-__device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
-                                             const double *__restrict__ aval, const int *__restrict__ brp,
-                                             const int *__restrict__ bre, const int *__restrict__ bcol,
-                                             const double *__restrict__ bval, int *cols, double *acc, int stride,
-                                             int cap, int *__restrict__ out_col,
-                                             double *__restrict__ out_val) {
+__device__ __forceinline__ int tiny_row_build(int a_lo, int a_hi, const int *__restrict__ acol,
+                                              const double *__restrict__ aval, const int *__restrict__ brp,
+                                              const int *__restrict__ bre, const int *__restrict__ bcol,
+                                              const double *__restrict__ bval, int *cols, double *acc, int stride,
+                                              int limit) {
     int n = 0, seen = 0;
     for (int p0 = a_lo; p0 < a_hi; p0 += TINY_BATCH) {
         TinyFetch<NC, true> F;
@@ -127,7 +109,7 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
         for (int u = 0; u < TINY_BATCH; u++) {
             const double a = F.a[u];
             for (int q = F.qs[u]; q < F.qe[u]; q++) {
-                if (++seen > TINY_MAX) return -1;
+                if (++seen > limit) return -1;
                 const bool first = q == F.qs[u];
                 const int j = first ? F.j0[u] : ldx<NC>(bcol + q);
                 const double pr = term<AR>(a, first ? F.b0[u] : ldx<NC>(bval + q));
@@ -147,11 +129,31 @@ __device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__re
             }
         }
     }
-    if (n > cap) return -1;
+    return n;
+}
+
+// copies a list built by tiny_row_build to out_col/out_val
+__device__ __forceinline__ void tiny_row_write(const int *cols, const double *acc, int stride, int n,
+                                               int *__restrict__ out_col, double *__restrict__ out_val) {
     for (int t = 0; t < n; t++) {
         out_col[t] = cols[t * stride];
         out_val[t] = acc[t * stride];
     }
+}
+
+// Fills the row's sorted columns and values at out_col/out_val and returns
+// its nnz; returns -1 on an inconsistency (more than TINY_MAX products, or
+// more than `cap` distinct columns).
+template <int AR, bool NC = true>
+__device__ __forceinline__ int tiny_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
+                                             const double *__restrict__ aval, const int *__restrict__ brp,
+                                             const int *__restrict__ bre, const int *__restrict__ bcol,
+                                             const double *__restrict__ bval, int *cols, double *acc, int stride,
+                                             int cap, int *__restrict__ out_col,
+                                             double *__restrict__ out_val) {
+    const int n = tiny_row_build<AR, NC>(a_lo, a_hi, acol, aval, brp, bre, bcol, bval, cols, acc, stride, TINY_MAX);
+    if (n < 0 || n > cap) return -1;
+    tiny_row_write(cols, acc, stride, n, out_col, out_val);
     return n;
 }
 
@@ -187,8 +189,11 @@ __device__ __forceinline__ void warp_row_extent(int a_lo, int a_hi, const int *_
     }
 }
 
-// OR the row's columns into msk[0..span) (tile t0 + i at msk[i]); false on a column outside the span
-template <bool NC = true>
+// OR the row's columns into msk[0..span) (tile t0 + i at msk[i]).  Without
+// CLIP a column outside the span is an error (returns false); with CLIP each
+// B row is first cut to the span's columns (two binary searches), so a wide
+// row can be taken one column window at a time.
+template <bool NC = true, bool CLIP = false>
 __device__ __forceinline__ bool warp_row_masks(int a_lo, int a_hi, const int *__restrict__ acol,
                                                const int *__restrict__ brp, const int *__restrict__ bre,
                                                const int *__restrict__ bcol, int t0,
@@ -196,7 +201,9 @@ __device__ __forceinline__ bool warp_row_masks(int a_lo, int a_hi, const int *__
     for (int t = lane_id(); t < span; t += WARP) msk[t] = 0ull;
     __syncwarp();
     bool bad = false;
-    warp_walk_tiles<false, NC>(a_lo, a_hi, 0, WARP, acol, brp, bre, bcol, 0, 0, [&](int q) {
+    const int c0 = CLIP ? t0 << 6 : 0;
+    const int c1 = CLIP ? (int)min((long long)(t0 + span) << 6, (long long)INT_MAX) : 0;
+    warp_walk_tiles<CLIP, NC>(a_lo, a_hi, 0, WARP, acol, brp, bre, bcol, c0, c1, [&](int q) {
         const int j = ldx<NC>(bcol + q);
         const int t = (j >> 6) - t0;
         if (t >= 0 && t < span) smem_setbit64(msk + t, j & 63);
@@ -216,7 +223,9 @@ __device__ __forceinline__ int warp_mask_count(const unsigned long long *msk, in
 // Given the row's masks: write its sorted columns to out_col, accumulate the
 // products (oracle order) in acc and write the values to out_val.  nnz must
 // equal the masks' popcount and be <= cap.  Returns false on inconsistency.
-template <int AR, bool NC = true>
+// CLIP: the masks cover one column window [t0*64, (t0+span)*64) of the row;
+// each B row is cut to it, and the output is that window's part of the row.
+template <int AR, bool NC = true, bool CLIP = false>
 __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__restrict__ acol,
                                               const double *__restrict__ aval, const int *__restrict__ brp,
                                               const int *__restrict__ bre, const int *__restrict__ bcol,
@@ -244,9 +253,15 @@ __device__ __forceinline__ bool warp_row_fill(int a_lo, int a_hi, const int *__r
     }
     for (int q = lane; q < nnz; q += WARP) acc[q] = 0.0;
     __syncwarp();
+    const int c0 = CLIP ? t0 << 6 : 0;
+    const int c1 = CLIP ? (int)min((long long)(t0 + span) << 6, (long long)INT_MAX) : 0;
     auto seg = [&](int, int k, int &elo, int &ehi) {
         elo = ldx<NC>(brp + k);
         ehi = ldx<NC>(bre + k);
+        if (CLIP) {
+            elo = lower_bound_x<NC>(bcol, elo, ehi, c0);
+            ehi = lower_bound_x<NC>(bcol, elo, ehi, c1);
+        }
     };
     auto lookup = [&](int j) -> int {
         const int t = (j >> 6) - t0;

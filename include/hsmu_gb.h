@@ -46,7 +46,7 @@ typedef enum hsmu_status {
     HSMU_ERR_INTERNAL = 6,     /* a device-side consistency check failed */
     HSMU_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up */
     HSMU_ERR_NO_DEVICE = 8,    /* no usable sm_103 device */
-    HSMU_ERR_UNSUPPORTED = 9,  /* a batch holds rows that need the plain engine's large-row path */
+    HSMU_ERR_UNSUPPORTED = 9,  /* kept for ABI stability; no call returns it */
     HSMU_ERR_CAPACITY = 10     /* hsmu_spgemm_host: output buffers too small (C->nnz = needed size) */
 } hsmu_status;
 
@@ -279,9 +279,11 @@ int hsmu_mlp_adam(float *params, const float *grad, float *m, float *v, float lr
  * one device pass and one host read; execute / graph_launch only enqueue
  * work (graph_launch captures the launch in a CUDA graph on first use and
  * replays it).  Results (hsmu_batch_result) are descriptors into the pool
- * (owned = 0) valid until hsmu_batch_destroy; rows of every product must fit
- * the warp path (tile span <= 512 tiles, <= 512 entries), otherwise
- * hsmu_batch_status reports HSMU_ERR_UNSUPPORTED. */
+ * (owned = 0) valid until hsmu_batch_destroy.  Rows of any width are taken:
+ * rows of more than 512 entries or a column span of more than 512 64-column
+ * tiles are written one column window at a time by a wide-row phase of the
+ * same launch.  A product whose entries exceed INT32_MAX reports
+ * HSMU_ERR_OVERFLOW. */
 #define HSMU_BATCH_PRODUCT 0
 #define HSMU_BATCH_GALERKIN 1
 typedef struct hsmu_batch_s *hsmu_batch;

@@ -2,7 +2,9 @@
 
 The batch must give, product by product, exactly what the oracle gives (the
 same summation order), through plain launches, CUDA-graph replays and after
-autotuning; rows it cannot take are reported, not computed wrongly."""
+autotuning, for rows of every width: thread rows, warp rows, and wide rows
+(more than 512 entries or a column span of more than 512 64-column tiles) that
+the launch's wide-row phase writes one column window at a time."""
 import numpy as np
 import pytest
 
@@ -129,7 +131,7 @@ def test_galerkin_batch_wide_intermediate_rows(engine, tiny):
         Pts.append(hsmu_gb.DeviceCSR.from_host(Pt))
     b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_GALERKIN, As, Ps, Pts)
     b.set_params(tiny)
-    for _ in range(2):  # the padded intermediate is rewritten on every launch
+    for _ in range(2):  # the intermediate is rewritten on every launch
         b.execute()
         b.status()
         for p, (A, P, Pt) in enumerate(host_ops):
@@ -140,13 +142,68 @@ def test_galerkin_batch_wide_intermediate_rows(engine, tiny):
             assert np.array_equal(C.val.view(np.int64), val.view(np.int64))
 
 
-def test_batch_reports_unsupported_rows(engine):
+def check_products(b, want):
+    for p, (rp, col, val) in enumerate(want):
+        C = host(b.result(p))
+        np.testing.assert_array_equal(C.row_ptr, rp.astype(np.int32))
+        np.testing.assert_array_equal(C.col, col)
+        assert np.array_equal(C.val.view(np.int64), val.view(np.int64)), "product %d" % p
+
+
+@pytest.mark.parametrize("tiny", [0, 32])
+def test_product_batch_wide_rows(engine, tiny):
+    # R-MAT scale 12 A*A (1,719 rows of more than 512 entries, up to 2,878), a product whose
+    # rows span up to ~4,700 tiles with ~100 products each, and small products between them
     import hsmu_gb
 
-    big = gen.rmat(12, 16, seed=2)  # rows wider than the warp path
-    d = hsmu_gb.DeviceCSR.from_host(big)
-    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_PRODUCT, [d], [d])
-    b.execute()
-    with pytest.raises(hsmu_gb.HsmuError) as ei:
+    rm = gen.rmat(12, 16, seed=2)
+    L = gen.poisson_random(2000, 20.0, seed=5, ncols=2000)
+    R = gen.poisson_random(2000, 5.0, seed=6, ncols=300000)
+    lap = gen.laplacian2d(30, seed=1)
+    pairs = [(lap, lap), (rm, rm), (L, R), (lap, lap), (rm, rm)]
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_PRODUCT, [hsmu_gb.DeviceCSR.from_host(x) for x, _ in pairs],
+                      [hsmu_gb.DeviceCSR.from_host(y) for _, y in pairs])
+    b.set_params(tiny)
+    want = [oracle.spgemm(x, y) for x, y in pairs]
+    for launch in ("execute", "graph", "graph"):
+        b.execute() if launch == "execute" else b.graph_launch()
         b.status()
-    assert ei.value.status == 9
+        check_products(b, want)
+    b.close()
+
+
+def test_product_batch_more_wide_rows_than_the_list(engine):
+    # 40 copies of R-MAT 12 A*A: 68,760 wide rows, more than the launch lists (65,536), so
+    # the rest are written in place by the warps that counted them
+    import hsmu_gb
+
+    rm = gen.rmat(12, 16, seed=2)
+    d = hsmu_gb.DeviceCSR.from_host(rm)
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_PRODUCT, [d] * 40, [d] * 40)
+    b.graph_launch()
+    b.status()
+    want = oracle.spgemm(rm, rm)
+    check_products(b, [want] * 40)
+    b.close()
+
+
+def test_galerkin_batch_wide_rows_in_both_products(engine):
+    # A*P rows of ~600 products over 40,000 columns (span ~625 tiles, ~595 entries) and
+    # Pt*(AP) rows of ~900 products: wide rows in the first and in the second product
+    import hsmu_gb
+
+    A = gen.poisson_random(2000, 20.0, seed=7, ncols=2000)
+    P = gen.poisson_random(2000, 30.0, seed=8, ncols=40000)
+    Pt = gen.transpose(P)
+    lap = gen.laplacian2d(20, seed=2)
+    lapP = gen.poisson_random(lap.M, 1.0, seed=9, ncols=50)
+    ops = [(A, P, Pt), (lap, lapP, gen.transpose(lapP))]
+    dev = hsmu_gb.DeviceCSR.from_host
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_GALERKIN, [dev(a) for a, _, _ in ops], [dev(x) for _, x, _ in ops],
+                      [dev(t) for _, _, t in ops])
+    want = [galerkin_oracle(*o) for o in ops]
+    for _ in range(2):
+        b.graph_launch()
+        b.status()
+        check_products(b, want)
+    b.close()
