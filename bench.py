@@ -802,7 +802,7 @@ def measure_batched(eng, name, steps, warmup):
            "plain_value": round(2.0 * products / (plain_ms * 1e-3) / 1e9, 3),
            "speedup_vs_plain": round(plain_ms / ms, 2), "autotuned": {"tiny": tiny, "grid": grid},
            "launches_per_step": 1, "graph": True,
-           "roofline": {"bound": "hbm", "kernel": "k_batch (persistent: both products, one pass each, chained scan per product)",
+           "roofline": {"bound": "hbm", "kernel": "k_batch (persistent: both products, one pass each, block allocation per tile)",
                         "achieved": round(gbs, 2), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
                         "peak_kind": peak_kind, "traffic": TRAFFIC.get(name), "alg_bytes": alg[0]},
            "parity": {"products_checked": pick, "bitwise": bitwise},
