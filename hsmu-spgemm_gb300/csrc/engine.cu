@@ -19,6 +19,7 @@
 #include <atomic>
 #include <initializer_list>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -71,15 +72,23 @@ const char *kErr[] = {"ok",
                       "internal consistency check failed on the device",
                       "bounded device wait timed out",
                       "no usable sm_103 device",
-                      "a batch holds rows that need the plain engine's large-row path",
+                      "unsupported (no call returns this status)",
                       "output buffers too small: C->nnz holds the required number of entries"};
 
 // hsmu_spgemm_host: output bytes (columns + values) per row panel, the most
-// panels, and the ratio of consecutive panel sizes (decreasing sizes: the copy
-// of the last panel, which nothing hides, is the smallest)
+// panels, and the growth of panel sizes from either end.  Panels grow by
+// HOST_PANEL_GROWTH from the first to the middle and shrink as much towards
+// the last: nothing hides the first panel's compute (the copy back starts
+// after it: what bounds a product whose output outruns the host link) or the
+// last panel's copy (what bounds a product whose compute is slower than the
+// link), so both are small.
 constexpr long long HOST_PANEL_BYTES = 32ll << 20;
-constexpr long long HOST_MAX_PANELS = 8;
-constexpr double HOST_PANEL_RATIO = 0.7;
+// learned path: the least share of the products in warp-class rows that may need (bounds
+// pass) or are predicted to need (after the prediction) numeric windows for the prediction
+// to be used
+constexpr double LEARNED_MIN_SHARE = 0.25;
+constexpr long long HOST_MAX_PANELS = 10;
+constexpr double HOST_PANEL_GROWTH = 2.0;
 
 int from_cuda(cudaError_t e) {
     if (e == cudaSuccess) return HSMU_OK;
@@ -602,14 +611,14 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
         np = np < 1 ? 1 : (np > HOST_MAX_PANELS ? HOST_MAX_PANELS : np);
         if (np > M) np = M > 0 ? M : 1;
         // panel q = rows [cut[q], cut[q+1]): the first row whose entries start at or after the
-        // panel's share of nnz; shares shrink geometrically (HOST_PANEL_RATIO) from the first panel
+        // panel's share of nnz; shares grow by HOST_PANEL_GROWTH from both ends to the middle
         cut.push_back(0);
-        double wsum = 0.0, w = 1.0;
-        for (long long q = 0; q < np; q++, w *= HOST_PANEL_RATIO) wsum += w;
+        std::vector<double> share((size_t)np);
+        double wsum = 0.0;
+        for (long long q = 0; q < np; q++) wsum += (share[q] = std::pow(HOST_PANEL_GROWTH, (double)std::min(q, np - 1 - q)));
         double acc = 0.0;
-        w = 1.0;
-        for (long long q = 1; q < np; q++, w *= HOST_PANEL_RATIO) {
-            acc += w;
+        for (long long q = 1; q < np; q++) {
+            acc += share[q - 1];
             const long long target = (long long)((double)nnz * (acc / wsum));
             const int row = (int)(std::lower_bound(C->row_ptr, C->row_ptr + M + 1, (int32_t)target) - C->row_ptr);
             cut.push_back(row < cut.back() ? cut.back() : (row > M ? M : row));
@@ -669,14 +678,17 @@ done:
 
 // Learned path (see learned.cu): predicted slots instead of the exact count pass.
 // B's tiles and the bounds pass are shared with the plain path (a PlainRun holds
-// them).  What the prediction saves is the count pass of the rows that take
-// numeric windows (large rows, and warp rows above FUSE_CAP entries); for every
-// other row the exact count is about as cheap as the prediction, and filling
-// speculative slots costs a compaction copy.  So the plain path finishes the
-// product on the same tiles and bounds when every row is tiny (known after the
-// bounds pass), or when no row is large and none is predicted above FUSE_CAP
-// entries (known after the prediction).  Either way the output is the plain
-// path's, bit for bit.
+// them).  What the prediction saves is the count pass of the warp-class rows
+// that take numeric windows (more than FUSE_CAP entries): their count is an OR
+// walk of its own.  Large rows are counted exactly either way (their count
+// builds the tile lists the structure pass streams); for every other row the
+// exact count is about as cheap as the prediction, and filling speculative
+// slots costs a compaction copy.  So the plain path finishes the product on
+// the same tiles and bounds unless warp-class rows of more than FUSE_CAP
+// products hold LEARNED_MIN_SHARE of the products (known after the bounds
+// pass) and the rows predicted above FUSE_CAP entries hold as much (known
+// after the prediction).  Either way the output is the plain path's, bit for
+// bit.
 int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_mlp *model,
                         const hsmu_opts *opts, cudaStream_t st, hsmu_stats *stats) {
     if (!h || !csr_ok(A) || !csr_ok(B) || !C || !model || !model->params) return HSMU_ERR_INVALID;
@@ -711,7 +723,13 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         rc = err_from_dev(hc.err);
         goto done;
     }
-    if (hc.bin_count[BIN_L] == 0 && hc.bin_count[BIN_DS] == 0) goto plain;
+    // what the prediction can save is the count pass of warp-class rows that need numeric
+    // windows: with few products in warp-class rows of more than FUSE_CAP products, the plain
+    // path finishes on the same tiles and bounds (large rows are counted exactly either way:
+    // their count builds their tile lists)
+    if (!o.learned_always &&
+        (hc.products == 0 || (double)hc.wide_ds_prod < LEARNED_MIN_SHARE * (double)hc.products))
+        goto plain;
     {
         // the large rows' tile lists: the arena is sized now, from the bounds pass's need
         if (r.ri.tcap && hc.bin_count[BIN_L] > 0) {
@@ -731,8 +749,8 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         CK(palloc(&soff, (size_t)M + 1, st));
         launch_features(r.Ad, r.Bd, feat, nullptr, h->nsm, st);
         // large rows with a tile list need no slot (they are written at their place in C)
-        launch_capacity(model->params, feat, r.ri.prod, M, B->N, model->margin, cap, h->nsm, st, &r.ctl->pred_wide,
-                        r.have_store ? r.ri.cls : nullptr);
+        launch_capacity(model->params, feat, r.ri.prod, r.ri.cls, M, B->N, model->margin, cap, h->nsm, st,
+                        &r.ctl->pred_wide_prod, r.have_store);
         launch_scan64(cap, soff, M, &r.ctl->nnz, r.scan_tmp, st);  // nnz field holds the slot total for now
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(h->h_ctl, r.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -742,7 +760,7 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
             rc = err_from_dev(hc.err);
             goto done;
         }
-        if (hc.bin_count[BIN_L] == 0 && hc.pred_wide == 0) goto plain;
+        if (!o.learned_always && (double)hc.pred_wide_prod < LEARNED_MIN_SHARE * (double)hc.products) goto plain;
         goto learned;
     }
 plain:

@@ -84,7 +84,9 @@ struct Ctl {
                                      // (bounds pass; for paths without a count pass)
     long long store_tiles;           // sum of RowInfo::tcap: arena entries the large rows could use
     long long store_used;            // arena entries reserved by the count pass
-    int pred_wide;                   // learned path: rows predicted above FUSE_CAP entries
+    unsigned long long wide_ds_prod; // products of warp-class rows with more than FUSE_CAP products
+    unsigned long long pred_wide_prod;  // learned path: products of warp-class rows predicted
+                                     // above FUSE_CAP entries
     long long win_listed;            // windows of the rows with a tile list (scan total)
 };
 

@@ -94,10 +94,12 @@ void launch_scan64(const int *in, long long *out, int n, long long *total64, int
 
 // learned.cu
 void launch_features(const DevCSR &A, const DevCSR &B, float4 *feat, long long *prod_out, int nsm, cudaStream_t st);
-// wide (nullable): incremented for every row predicted clearly above FUSE_CAP entries;
-// cls (nullable): rows of the large class get no slot (the caller keeps their tile lists)
-void launch_capacity(const float *params, const float4 *feat, const long long *prod, int M, int N, float margin,
-                     int *cap, int nsm, cudaStream_t st, int *wide = nullptr, const signed char *cls = nullptr);
+// wide_prod (nullable): incremented by the products of every warp-class row predicted clearly
+// above FUSE_CAP entries; large_no_slot: rows of the large class get no slot (the caller keeps
+// their tile lists)
+void launch_capacity(const float *params, const float4 *feat, const long long *prod, const signed char *cls, int M,
+                     int N, float margin, int *cap, int nsm, cudaStream_t st, unsigned long long *wide_prod,
+                     bool large_no_slot);
 void launch_compact(int M, const long long *soff, const int *crp, const unsigned char *flag, const int *scol,
                     const double *sval, int *ccol, double *cval, int nsm, cudaStream_t st);
 

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     __shared__ int s_cnt[NBIN];
     const int sub = threadIdx.x & (G - 1);
     const int rloc = threadIdx.x / G;
-    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0, my_tc = 0;
+    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0, my_tc = 0, my_wdp = 0;
     if (threadIdx.x < NBIN) s_cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int rb = blockIdx.x * RPB; rb < M; rb += gridDim.x * RPB) {
@@ -77,7 +77,10 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                 my_wb += wb;
                 // rows that can reach the window pass: the large class, and warp rows above FUSE_CAP
                 if (bin == BIN_L) my_cb += wb * (unsigned long long)(arp[i + 1] - arp[i]);
-                if (bin == BIN_DS && prod > FUSE_CAP) my_cbd += wb * (unsigned long long)(arp[i + 1] - arp[i]);
+                if (bin == BIN_DS && prod > FUSE_CAP) {
+                    my_cbd += wb * (unsigned long long)(arp[i + 1] - arp[i]);
+                    my_wdp += (unsigned long long)prod;
+                }
             }
             ri.cls[i] = (signed char)bin;
             if (ri.tcap) {
@@ -96,7 +99,9 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     my_cb = warp_sum(my_cb);
     my_cbd = warp_sum(my_cbd);
     my_tc = warp_sum(my_tc);
+    my_wdp = warp_sum(my_wdp);
     if (lane_id() == 0) {
+        if (my_wdp) atomicAdd(&ctl->wide_ds_prod, my_wdp);
         if (my_tc) atomicAdd(reinterpret_cast<unsigned long long *>(&ctl->store_tiles), my_tc);
         if (my_prod) atomicAdd(&ctl->products, my_prod);
         if (my_wb) atomicAdd(&ctl->win_bound, my_wb);

@@ -238,13 +238,18 @@ __global__ void k_adam(float *__restrict__ params, const float *__restrict__ gra
 
 // ---------------------------------------------------------------- speculative slots
 // capacity of row i: exact bound for rows with <= TINY_MAX products (they
-// always fit), min(products, N, 2^(prediction + margin)) otherwise.
+// always fit), min(products, N, 2^(prediction + margin)) otherwise; large rows
+// that keep a tile list take none (large_no_slot).  wide_prod: the products of
+// the warp-class rows predicted clearly wider than the fused warp path (what
+// the prediction can save is their count pass).
 __global__ void __launch_bounds__(256) k_capacity(const float *__restrict__ params, const float4 *__restrict__ feat,
                                                   const long long *__restrict__ prod, int M, int N, float margin,
-                                                  int *__restrict__ cap, int *wide,
-                                                  const signed char *__restrict__ cls) {
+                                                  int *__restrict__ cap, unsigned long long *wide_prod,
+                                                  const signed char *__restrict__ cls, bool large_no_slot) {
     __shared__ float P[MLP_NTOTAL];
+    __shared__ unsigned long long s_wide;
     for (int q = threadIdx.x; q < MLP_NTOTAL; q += blockDim.x) P[q] = params[q];
+    if (threadIdx.x == 0) s_wide = 0;
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
         const long long pr = prod[i];
@@ -260,14 +265,13 @@ __global__ void __launch_bounds__(256) k_capacity(const float *__restrict__ para
             if (c < 1) c = 1;
             w = y > log2f((float)FUSE_CAP) + 0.5f && bound > FUSE_CAP;  // half a step of slack
         }
-        if (cls && cls[i] == BIN_L) c = 0;  // a large row with a tile list takes no slot
+        const bool large = cls[i] == BIN_L;
+        if (large && large_no_slot) c = 0;  // a large row with a tile list takes no slot
         cap[i] = (int)c;
-        // such rows go through numeric windows
-        if (wide) {
-            const unsigned m = __ballot_sync(__activemask(), w);
-            if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(wide, __popc(m));
-        }
+        if (w && !large) atomicAdd(&s_wide, (unsigned long long)pr);
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_wide && wide_prod) atomicAdd(wide_prod, s_wide);
 }
 
 // copy rows fused in their speculative slots (columns and values, at most a
@@ -290,9 +294,10 @@ __global__ void __launch_bounds__(256) k_compact(int M, const long long *__restr
     }
 }
 
-void launch_capacity(const float *params, const float4 *feat, const long long *prod, int M, int N, float margin,
-                     int *cap, int nsm, cudaStream_t st, int *wide, const signed char *cls) {
-    k_capacity<<<nsm * 4, 256, 0, st>>>(params, feat, prod, M, N, margin, cap, wide, cls);
+void launch_capacity(const float *params, const float4 *feat, const long long *prod, const signed char *cls, int M,
+                     int N, float margin, int *cap, int nsm, cudaStream_t st, unsigned long long *wide_prod,
+                     bool large_no_slot) {
+    k_capacity<<<nsm * 4, 256, 0, st>>>(params, feat, prod, M, N, margin, cap, wide_prod, cls, large_no_slot);
 }
 
 void launch_compact(int M, const long long *soff, const int *crp, const unsigned char *flag, const int *scol,

@@ -75,7 +75,7 @@ class c_btiles(ctypes.Structure):
 class c_opts(ctypes.Structure):
     _fields_ = [("validate", ctypes.c_int32), ("arith", ctypes.c_int32),
                 ("window_cap", ctypes.c_int32), ("panels", ctypes.c_int32), ("wait_polls", ctypes.c_int32),
-                ("no_tile_store", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+                ("no_tile_store", ctypes.c_int32), ("learned_always", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class c_mlp(ctypes.Structure):
@@ -404,11 +404,13 @@ class Engine:
             pass
 
     def spgemm_learned(self, A: DeviceCSR, B: DeviceCSR, params, margin: float, *, arith: int = 0,
-                       validate: bool = False, stream=None, stats: bool = False, wait_polls: int = 0) -> DeviceCSR:
-        """C = A * B with predicted row slots (hsmu_spgemm_learned); params: device float tensor."""
+                       validate: bool = False, stream=None, stats: bool = False, wait_polls: int = 0,
+                       always: bool = False) -> DeviceCSR:
+        """C = A * B with predicted row slots (hsmu_spgemm_learned); params: device float tensor.
+        always (a test hook): use the prediction even where the plain path would be chosen."""
         L = load_library()
         C = c_csr()
-        o = c_opts(int(validate), int(arith), 0, 0, int(wait_polls))
+        o = c_opts(int(validate), int(arith), 0, 0, int(wait_polls), 0, int(always))
         m = c_mlp(params.data_ptr(), float(margin), 0)
         st = c_stats()
         rc = L.hsmu_spgemm_learned(self.handle, ctypes.byref(A.desc), ctypes.byref(B.desc), ctypes.byref(C),

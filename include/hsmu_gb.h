@@ -99,7 +99,8 @@ typedef struct hsmu_opts {
                            * deterministic; RN and IMUL give identical bits. */
     int32_t window_cap;   /* 0: default slots per numeric window (<= 4096) */
     int32_t panels;       /* hsmu_spgemm_host: row panels of the copy pipeline (0: one per 32 MB
-                           * of output; at most 8), sized in a decreasing geometric series */
+                           * of output; at most 10); sizes double from the first panel to the
+                           * middle and halve towards the last */
     int32_t wait_polls;   /* test hook, 0 in normal use.  > 0: every bounded device wait of the call
                            * gives up after this many polls instead of its default limit (the value
                            * pass's wait for a window's column copy polls without blocking; the batch's
@@ -109,7 +110,9 @@ typedef struct hsmu_opts {
                            * it applies to every launch of the batch. */
     int32_t no_tile_store; /* 1: the count pass keeps no C tiles of the large rows, and the structure
                            * pass repeats their OR walk over B's tiles (same output; less scratch) */
-    int32_t reserved[2];
+    int32_t learned_always; /* test hook, 0 in normal use.  1: hsmu_spgemm_learned never hands the
+                           * product to the plain path (it uses its prediction whatever the rows) */
+    int32_t reserved;
 } hsmu_opts;
 
 /* Per-call statistics (filled by hsmu_spgemm when stats != NULL). */

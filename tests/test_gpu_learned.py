@@ -83,7 +83,7 @@ def model_for_tests(engine):
     return p, learned.choose_margin(p, X, y, 0.99)
 
 
-def run_both(engine, A, B, params, margin):
+def run_both(engine, A, B, params, margin, always=False):
     import torch
 
     import hsmu_gb
@@ -92,13 +92,16 @@ def run_both(engine, A, B, params, margin):
     dB = dA if B is A else hsmu_gb.DeviceCSR.from_host(B)
     P = engine.spgemm(dA, dB).to_host()
     pt = torch.from_numpy(np.ascontiguousarray(params, np.float32)).cuda()
-    Cd = engine.spgemm_learned(dA, dB, pt, margin, stats=True)
+    Cd = engine.spgemm_learned(dA, dB, pt, margin, stats=True, always=always)
     st = engine.last_stats
     return P, Cd.to_host(), st
 
 
+@pytest.mark.parametrize("always", [False, True])
 @pytest.mark.parametrize("name", ["lap", "st27", "rmat12", "rmat13T", "rect", "wide"])
-def test_learned_identical_to_plain(engine, name):
+def test_learned_identical_to_plain(engine, name, always):
+    # always: the prediction is used whatever the rows (the routing to the plain path is off),
+    # so the speculative passes run on every input
     p, margin = model_for_tests(engine)
     if name == "lap":
         A = B = gen.laplacian2d(64, seed=0)
@@ -115,11 +118,13 @@ def test_learned_identical_to_plain(engine, name):
     else:
         A = gen.poisson_random(400, 40, seed=7, ncols=2000)
         B = gen.poisson_random(2000, 60, seed=8, ncols=1_200_000)
-    P, C, st = run_both(engine, A, B, p, margin)
+    P, C, st = run_both(engine, A, B, p, margin, always)
     np.testing.assert_array_equal(C.row_ptr, P.row_ptr)
     np.testing.assert_array_equal(C.col, P.col)
     assert np.array_equal(C.val.view(np.int64), P.val.view(np.int64))
     assert st["nnz_c"] == P.nnz
+    if always:
+        assert st["routed"] == 0
 
 
 def test_learned_fma_mode(engine):
@@ -156,18 +161,21 @@ def test_trained_model_sizes_slots_tighter_than_the_bound(engine):
     # what the network gains: slot memory close to nnz(C), instead of the product-count bound
     p, margin = model_for_tests(engine)
     A = gen.stencil27(14, 3, seed=1)
-    P, C, st = run_both(engine, A, A, p, margin)
+    P, C, st = run_both(engine, A, A, p, margin, always=True)
     prods = gen.products(A, A)
     assert st["spec_capacity"] < 0.25 * prods           # the bound would allocate `prods` entries
     assert st["fallback_rows"] <= 0.15 * A.M            # boundary rows of a small grid are the hardest
 
 
-@pytest.mark.parametrize("name", ["lap", "st27"])
-def test_inputs_without_windowed_rows_go_to_the_plain_path(engine, name):
-    # every row tiny (Laplacian), or no large row and none predicted above the fused
-    # warp path (stencil): the plain path finishes the product on the same tiles
+@pytest.mark.parametrize("name", ["lap", "st27", "rmat16"])
+def test_inputs_the_prediction_cannot_help_go_to_the_plain_path(engine, name):
+    # every row tiny (Laplacian); warp rows none of which is predicted above the fused warp
+    # path (stencil); wide rows all of the large class, whose exact count builds the tile
+    # lists the structure pass streams (R-MAT scale 16, 1,024 tiles of columns): the plain
+    # path finishes the product on the same tiles and bounds
     p, margin = model_for_tests(engine)
-    A = gen.laplacian2d(96, seed=0) if name == "lap" else gen.stencil27(12, 3, seed=1)
+    A = {"lap": lambda: gen.laplacian2d(96, seed=0), "st27": lambda: gen.stencil27(12, 3, seed=1),
+         "rmat16": lambda: gen.rmat(16, 16, seed=2)}[name]()
     P, C, st = run_both(engine, A, A, p, margin)
     assert st["routed"] == 1
     np.testing.assert_array_equal(C.row_ptr, P.row_ptr)
