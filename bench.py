@@ -474,6 +474,9 @@ def measure_plain(eng, A, B, name, steps, warmup, arith, world=1, rank=0, local=
         kname, kms = "k_numeric (values, per window)", nu_ms
     achieved = alg_bytes / (kms * 1e-3) / 1e9
     products_mine = gen.products(Ah, B)
+    # diagnostic, not the graded figure: every product gathers its B entry (12 bytes), plus the
+    # A and C terms
+    gather_bytes = 12 * products_mine + csr_bytes(Ah.M, Ah.nnz) + csr_bytes(Ah.M, nnz_c)
     fp64_per_product = {"rn": 2.0, "fma": 1.0, "imul": 1.0}[arith]
     return {
         "ms": ms, "value": value, "nnz_c": nnz_c, "products": products_total, "products_rank": products_mine,
@@ -482,7 +485,8 @@ def measure_plain(eng, A, B, name, steps, warmup, arith, world=1, rank=0, local=
         "alg_bytes": alg_bytes,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name),
-                     "alg_bytes": alg_bytes, "ms": round(kms, 4)},
+                     "alg_bytes": alg_bytes, "ms": round(kms, 4), "gather_bytes": gather_bytes,
+                     "gather_gbs": round(gather_bytes / (kms * 1e-3) / 1e9, 2)},
         "fp64_ops": fp64_per_product * products_mine, "kernel_ms": kms,
         "e2e": {"value": round(e2e_value, 3), "unit": "GFLOPS", "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
