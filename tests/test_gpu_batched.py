@@ -207,3 +207,37 @@ def test_galerkin_batch_wide_rows_in_both_products(engine):
         b.status()
         check_products(b, want)
     b.close()
+
+
+def test_product_batch_degenerate_products(engine):
+    # a product without rows, one whose rows are all empty, a 1x1 product, one row past a
+    # tile of 32, and rows whose A entries all point at empty B rows, in one launch
+    import hsmu_gb
+
+    def csr(M, N, rows):
+        rp = np.zeros(M + 1, np.int32)
+        col, val = [], []
+        for i, r in enumerate(rows):
+            for c, v in r:
+                col.append(c)
+                val.append(v)
+            rp[i + 1] = len(col)
+        rp[len(rows) + 1:] = len(col)
+        return gen.CSR(M, N, rp, np.array(col, np.int32), np.array(val, np.float64))
+
+    empty_rows_B = csr(6, 9, [[(1, 2.0)], [], [(3, -1.0), (8, 0.5)], [], [], [(0, 1.5)]])
+    pairs = [
+        (csr(0, 10, []), gen.poisson_random(10, 3.0, seed=1)),
+        (csr(50, 40, []), gen.poisson_random(40, 3.0, seed=2, ncols=30)),
+        (csr(1, 1, [[(0, 2.0)]]), csr(1, 1, [[(0, 3.0)]])),
+        (gen.poisson_random(33, 4.0, seed=3), gen.poisson_random(33, 4.0, seed=4)),
+        (csr(4, 6, [[(1, 1.0), (3, 2.0)], [(4, 1.0)], [(0, 1.0), (1, 1.0)], []]), empty_rows_B),
+    ]
+    dev = hsmu_gb.DeviceCSR.from_host
+    b = hsmu_gb.Batch(engine, hsmu_gb.BATCH_PRODUCT, [dev(x) for x, _ in pairs], [dev(y) for _, y in pairs])
+    want = [oracle.spgemm(x, y) for x, y in pairs]
+    for _ in range(2):
+        b.graph_launch()
+        b.status()
+        check_products(b, want)
+    b.close()
