@@ -53,8 +53,7 @@ struct hsmu_handle_s {
     // tile store arena (C tiles of the large rows, kept by the count pass): grown, up to
     // STORE_MAX_TILES, to the largest need a call has reported, before the next call
     int *arena_col;
-    unsigned long long *arena_mask;
-    long long *arena_info;
+    TileEnt *arena_ent;
     long long arena_cap, arena_want;
     // host-buffer entry: copy streams and their ordering events
     cudaStream_t cs_in, cs_out;
@@ -323,16 +322,13 @@ struct PlainRun {
         if (h->arena_want <= h->arena_cap) return cudaSuccess;
         const long long want = std::min(h->arena_want, STORE_MAX_TILES);
         pfree(h->arena_col, st);
-        pfree(h->arena_mask, st);
-        pfree(h->arena_info, st);
+        pfree(h->arena_ent, st);
         h->arena_cap = 0;
         cudaError_t e = palloc(&h->arena_col, (size_t)want, st);
-        if (e == cudaSuccess) e = palloc(&h->arena_mask, (size_t)want, st);
-        if (e == cudaSuccess) e = palloc(&h->arena_info, (size_t)want, st);
+        if (e == cudaSuccess) e = palloc(&h->arena_ent, (size_t)want, st);
         if (e != cudaSuccess) {
             pfree(h->arena_col, st);
-            pfree(h->arena_mask, st);
-            pfree(h->arena_info, st);
+            pfree(h->arena_ent, st);
             h->arena_want = 0;
             return e;
         }
@@ -395,7 +391,7 @@ struct PlainRun {
 
     TileStore store_view() const {
         return TileStore{ts_off,        ts_cnt,       ts_nwin,       reserve_windows ? ts_wbase : nullptr,
-                         h->arena_col,  h->arena_mask, h->arena_info, h->arena_cap,
+                         h->arena_col, h->arena_ent, h->arena_cap,
                          (int)(hc.store_used <= h->arena_cap)};
     }
 
@@ -834,7 +830,7 @@ learned:
         // counts), before any warp row's window: the value pass hands windows out in array
         // order, and R-MAT's heaviest rows come first.  The redo pass then streams those rows
         // without barriers.
-        TileStore tsd{r.ts_off, r.ts_cnt, r.ts_nwin, r.ts_wbase, h->arena_col, h->arena_mask, h->arena_info,
+        TileStore tsd{r.ts_off, r.ts_cnt, r.ts_nwin, r.ts_wbase, h->arena_col, h->arena_ent,
                       h->arena_cap, 0};
         const int small_rows[NBIN] = {hc.bin_count[BIN_DS], 0, hc.bin_count[BIN_TINY]};
         const int large_rows[NBIN] = {0, hc.bin_count[BIN_L], 0};
@@ -1138,9 +1134,9 @@ int hsmu_handle_destroy(hsmu_handle h) {
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out})
         if (e) cudaEventDestroy(e);
-    if (h->arena_col || h->arena_mask || h->arena_info) {
+    if (h->arena_col || h->arena_ent) {
         cudaDeviceSynchronize();  // no call of this handle still reads the arena
-        for (void *p : {(void *)h->arena_col, (void *)h->arena_mask, (void *)h->arena_info})
+        for (void *p : {(void *)h->arena_col, (void *)h->arena_ent})
             if (p) cudaFreeAsync(p, 0);
         cudaStreamSynchronize(0);
     }

@@ -55,10 +55,19 @@ struct RowInfo {
 // C tiles of the large-class rows, kept by the count pass (which builds them
 // anyway) so that the structure pass streams each row's tile list instead of
 // repeating the OR walk over B's tiles.  Each large row reserves RowInfo::tcap
-// entries of the arena (tcol/tmask, `cap` entries, owned by the handle) with
+// entries of the arena (tcol/tent, `cap` entries, owned by the handle) with
 // one atomic; a row that finds the arena full keeps nothing (cnt[i] = -1) and
 // the structure pass walks B for it as before.  Row i's list:
-// tcol/tmask[off[i] .. off[i] + cnt[i]), tile ids ascending.
+// tcol/tent[off[i] .. off[i] + cnt[i]), tile ids ascending.
+//
+// A tile's column mask and its slot word are written and read together, so
+// they share one 16-byte entry: one 128-bit store in the count pass, one
+// 128-bit load in the structure pass.
+struct alignas(16) TileEnt {
+    unsigned long long mask;    // column mask
+    long long info;             // first slot | (window ordinal + 1) << 32 (hsmu_tilelist.cuh)
+};
+
 struct TileStore {
     long long *off;             // [M] written by the count pass
     int *cnt;                   // [M] tiles stored per row, -1: none
@@ -66,8 +75,7 @@ struct TileStore {
     int *wbase;                 // [M+1] index of the row's first window: exclusive scan of nwin in row
                                 // order (nullable: the structure pass reserves them itself)
     int *tcol;                  // arena: tile ids
-    unsigned long long *tmask;  // arena: column masks
-    long long *tinfo;           // arena: first slot | (window ordinal + 1) << 32 (hsmu_tilelist.cuh)
+    TileEnt *tent;              // arena: column mask and slot word of each tile
     long long cap;              // arena entries
     int all_stored;             // host: every large row got a list (no OR-walk rows left)
 };

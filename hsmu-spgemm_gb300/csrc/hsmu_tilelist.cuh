@@ -3,10 +3,10 @@
 // tile masks); chunk_to_list turns that table into the row's list of
 // non-empty tiles, in column order, with everything the structure pass needs
 // to write the row without any scan of its own:
-//   tcol  tile id,
-//   tmask column mask,
-//   tinfo (first slot of the tile in the row) | ((window ordinal + 1) << 32)
-//         for a tile that starts a numeric window (0 in the high word otherwise).
+//   tcol       tile id,
+//   tent.mask  column mask,
+//   tent.info  (first slot of the tile in the row) | ((window ordinal + 1) << 32)
+//              for a tile that starts a numeric window (0 in the high word otherwise).
 // Windows are cut where a tile's first slot crosses a multiple of WIN_CUT, its
 // rank among the row's tiles crosses a multiple of WIN_TCAP, or its offset
 // from the row's first tile crosses a multiple of WIN_SPAN -- the limits of
@@ -21,6 +21,7 @@
 // starts) give every warp its place in the row.
 #pragma once
 #include "hsmu_block.cuh"
+#include "hsmu_kernels.h"
 
 namespace hsmu {
 
@@ -55,8 +56,7 @@ struct ListSmem {
 // false (nothing written) if the chunk's tiles would go past `cap` entries.
 template <int NW>
 __device__ bool chunk_to_list(const unsigned long long *msk, int len, int c0, int tmin, ListRun &run, ListSmem<NW> &sm,
-                              long long base, int cap, int *__restrict__ out_col,
-                              unsigned long long *__restrict__ out_mask, long long *__restrict__ out_info) {
+                              long long base, int cap, int *__restrict__ out_col, TileEnt *__restrict__ out_ent) {
     const int lane = lane_id(), w = threadIdx.x >> 5;
     const int wspan = (((len + NW - 1) / NW) + WARP - 1) & ~(WARP - 1);
     const int w0 = min(len, w * wspan), w1 = min(len, w0 + wspan);
@@ -101,8 +101,7 @@ __device__ bool chunk_to_list(const unsigned long long *msk, int len, int c0, in
             if (m) {
                 const long long at = pos + __popc(nz & lanemask_lt());
                 out_col[at] = c0 + t;
-                out_mask[at] = m;
-                out_info[at] = (long long)(unsigned)(s_run + incl - pc);
+                out_ent[at] = TileEnt{m, (long long)(unsigned)(s_run + incl - pc)};
             }
             pos += __popc(nz);
             s_run += __shfl_sync(FULL, incl, WARP - 1);
@@ -115,7 +114,7 @@ __device__ bool chunk_to_list(const unsigned long long *msk, int len, int c0, in
     const int qa = min(tot_ne, w * per), qb = min(tot_ne, qa + per);
     auto key_at = [&](int q) -> long long {  // key of chunk entry q (row rank run.tiles + q)
         const long long at = base + run.tiles + q;
-        return win_key_row((int)(unsigned)out_info[at], run.tiles + q, out_col[at] - tmin);
+        return win_key_row((int)(unsigned)out_ent[at].info, run.tiles + q, out_col[at] - tmin);
     };
     long long kin = run.key;
     if (fits && qa < qb && qa > 0) kin = key_at(qa - 1);
@@ -132,7 +131,7 @@ __device__ bool chunk_to_list(const unsigned long long *msk, int len, int c0, in
             if (wr && start) {
                 const long long at = base + run.tiles + q;
                 const long long ord1 = (long long)(ob + starts + __popc(sbits & lanemask_lt()) + 1);
-                out_info[at] = (ord1 << 32) | (long long)(unsigned)out_info[at];
+                out_ent[at].info = (ord1 << 32) | (long long)(unsigned)out_ent[at].info;
             }
             starts += __popc(sbits);
             kprev = __shfl_sync(FULL, key, min(WARP, qb - q0) - 1);

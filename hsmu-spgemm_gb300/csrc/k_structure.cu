@@ -444,8 +444,11 @@ __global__ void __launch_bounds__(SLS_THREADS, 6) k_struct_ls(int M, RowInfo ri,
                 const int q = q0 + lane;
                 const bool v = q < n;
                 const int t = v ? __ldg(ts.tcol + sb + q) : 0;
-                const unsigned long long m = v ? __ldg(ts.tmask + sb + q) : 0ull;
-                const long long info = v ? __ldg(ts.tinfo + sb + q) : 0ll;
+                // the tile's mask and slot word: one 128-bit load
+                const ulonglong2 e = v ? __ldg(reinterpret_cast<const ulonglong2 *>(ts.tent) + sb + q)
+                                       : make_ulonglong2(0ull, 0ull);
+                const unsigned long long m = e.x;
+                const long long info = (long long)e.y;
                 const int slot = (int)(unsigned)info;
                 const int ord1 = (int)(info >> 32);
                 if (ord1) {

@@ -135,8 +135,7 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
             if (STORE && sbase >= 0) {
                 // the chunk's non-empty tiles appended to the row's list, with their slots
                 // and window starts (hsmu_tilelist.cuh)
-                if (!chunk_to_list<NWARP>(msk, c1 - c0, c0, tmin, run, s_ls, sbase, scap, ts.tcol, ts.tmask,
-                                          ts.tinfo) &&
+                if (!chunk_to_list<NWARP>(msk, c1 - c0, c0, tmin, run, s_ls, sbase, scap, ts.tcol, ts.tent) &&
                     threadIdx.x == 0)
                     set_err(&ctl->err, DERR_INTERNAL);
                 total = run.slots;
@@ -195,7 +194,7 @@ void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, Ro
 void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,
                         cudaStream_t st) {
     const size_t smem = DCH_COUNT * sizeof(unsigned long long);
-    if (ts && ts->tcol && ts->tinfo && ts->cap > 0 && ri.tcap)
+    if (ts && ts->tcol && ts->tent && ts->cap > 0 && ri.tcap)
         k_count_l<LM_STORE><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, *ts,
                                                                RowOut{}, ctl);
     else
