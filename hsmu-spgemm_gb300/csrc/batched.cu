@@ -66,6 +66,8 @@ struct BOp {  // one CSR operand on the device; row k is rp[k] .. re[k]-1
     const double *val;
 };
 
+// A round: one product of every entry of the batch (one round for plain products;
+// two for Galerkin entries, A*P and then Pt*(AP)).
 struct BRound {
     int nprod;
     const BOp *A;            // left operand per product
@@ -513,8 +515,8 @@ __global__ void __launch_bounds__(BW * 32, 2) k_batch(BParams P) {
     extern __shared__ unsigned long long s_dyn[];
     BWarpSmem &S = reinterpret_cast<BWarpSmem *>(s_dyn)[threadIdx.x >> 5];
     for (int r = 0; r < P.nrounds; r++) {
-        // round 0 reads only the caller's operands (read-only path); later rounds read
-        // the previous round's output through L2
+        // the first product reads only the caller's operands (read-only path); the second
+        // reads the first one's output through L2
         if (r == 0) phase_tiles<AR, true>(P, r, S);
         else phase_tiles<AR, false>(P, r, S);
         if (!grid_sync(P.bar, P.err, P.spin_limit)) return;
@@ -539,7 +541,7 @@ __global__ void __launch_bounds__(BW * 32, 2) k_batch(BParams P) {
 }
 
 // ---------------------------------------------------------------- sizing
-// per row of round 1: products and the bound min(products, N) on its nnz,
+// per row of the first product: products and the bound min(products, N) on its nnz,
 // summed per product; `rowbound` keeps the uncapped products of each row for
 // the second product's bound
 __device__ __forceinline__ void add_per_product(unsigned long long *pbound, int p, unsigned long long v) {
