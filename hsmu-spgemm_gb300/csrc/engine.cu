@@ -75,19 +75,24 @@ const char *kErr[] = {"ok",
                       "output buffers too small: C->nnz holds the required number of entries"};
 
 // hsmu_spgemm_host: output bytes (columns + values) per row panel, the most
-// panels, and the growth of panel sizes from either end.  Panels grow by
-// HOST_PANEL_GROWTH from the first to the middle and shrink as much towards
-// the last: nothing hides the first panel's compute (the copy back starts
-// after it: what bounds a product whose output outruns the host link) or the
-// last panel's copy (what bounds a product whose compute is slower than the
-// link), so both are small.
+// panels, and how panel sizes follow each other.  Nothing hides the first
+// panel's compute (the copy back starts after it) or the last panel's copy.
+// A product whose output outruns the host link (more than HOST_LINK_BOUND
+// output bytes per intermediate product: the copy takes longer than the
+// compute) starts small and grows by HOST_PANEL_GROWTH to the middle, then
+// shrinks as much; one whose compute is the longer part only needs a small
+// last panel, and its sizes shrink by HOST_PANEL_RATIO from the first (small
+// panels leave the GPU partly idle, so only one end is made small).
 constexpr long long HOST_PANEL_BYTES = 32ll << 20;
+constexpr long long HOST_MAX_PANELS = 8;
+constexpr double HOST_PANEL_GROWTH = 2.0;
+constexpr double HOST_PANEL_RATIO = 0.7;
+constexpr double HOST_LINK_BOUND = 1.5;
+
 // learned path: the least share of the products in warp-class rows that may need (bounds
 // pass) or are predicted to need (after the prediction) numeric windows for the prediction
 // to be used
 constexpr double LEARNED_MIN_SHARE = 0.25;
-constexpr long long HOST_MAX_PANELS = 10;
-constexpr double HOST_PANEL_GROWTH = 2.0;
 
 int from_cuda(cudaError_t e) {
     if (e == cudaSuccess) return HSMU_OK;
@@ -607,11 +612,14 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
         np = np < 1 ? 1 : (np > HOST_MAX_PANELS ? HOST_MAX_PANELS : np);
         if (np > M) np = M > 0 ? M : 1;
         // panel q = rows [cut[q], cut[q+1]): the first row whose entries start at or after the
-        // panel's share of nnz; shares grow by HOST_PANEL_GROWTH from both ends to the middle
+        // panel's share of nnz
         cut.push_back(0);
+        const bool link_bound = 12.0 * (double)nnz > HOST_LINK_BOUND * (double)r.hc.products;
         std::vector<double> share((size_t)np);
         double wsum = 0.0;
-        for (long long q = 0; q < np; q++) wsum += (share[q] = std::pow(HOST_PANEL_GROWTH, (double)std::min(q, np - 1 - q)));
+        for (long long q = 0; q < np; q++)
+            wsum += (share[q] = link_bound ? std::pow(HOST_PANEL_GROWTH, (double)std::min(q, np - 1 - q))
+                                           : std::pow(HOST_PANEL_RATIO, (double)q));
         double acc = 0.0;
         for (long long q = 1; q < np; q++) {
             acc += share[q - 1];

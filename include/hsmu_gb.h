@@ -99,8 +99,10 @@ typedef struct hsmu_opts {
                            * deterministic; RN and IMUL give identical bits. */
     int32_t window_cap;   /* 0: default slots per numeric window (<= 4096) */
     int32_t panels;       /* hsmu_spgemm_host: row panels of the copy pipeline (0: one per 32 MB
-                           * of output; at most 10); sizes double from the first panel to the
-                           * middle and halve towards the last */
+                           * of output; at most 8).  Sizes shrink from the first panel when the
+                           * compute takes longer than the copy back; when the copy is the longer
+                           * part they double from the first panel to the middle and halve
+                           * towards the last */
     int32_t wait_polls;   /* test hook, 0 in normal use.  > 0: every bounded device wait of the call
                            * gives up after this many polls instead of its default limit (the value
                            * pass's wait for a window's column copy polls without blocking; the batch's
