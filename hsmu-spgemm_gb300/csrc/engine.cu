@@ -329,7 +329,8 @@ struct PlainRun {
         pfree(h->arena_col, st);
         pfree(h->arena_ent, st);
         h->arena_cap = 0;
-        cudaError_t e = palloc(&h->arena_col, (size_t)want, st);
+        // 4 ints of slack: the value pass fetches a window's tile ids in 16-byte units
+        cudaError_t e = palloc(&h->arena_col, (size_t)want + 4, st);
         if (e == cudaSuccess) e = palloc(&h->arena_ent, (size_t)want, st);
         if (e != cudaSuccess) {
             pfree(h->arena_col, st);
@@ -413,8 +414,9 @@ struct PlainRun {
     // of the large class or a warp row above FUSE_CAP exists)
     void values() {
         if (hc.nnz == 0 || win_cap == 0 || (hc.bin_count[BIN_L] == 0 && hc.wide_rows == 0)) return;
+        const TileStore tsd = store_view();
         launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, wc, ctl, o.arith, h->nsm,
-                       st, o.wait_polls);
+                       st, o.wait_polls, have_store ? &tsd : nullptr);
         launches += 6;  // window lengths, 3 scan, cursors, values
     }
 
@@ -872,7 +874,7 @@ learned:
                          win_cap, ctl, o.arith, h->nsm, st, nullptr, r.have_store ? &tsd : nullptr);
         if (stats) cudaEventRecord(h->ev[4], st);
         launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, flag, scol, soff, wc, ctl, o.arith, h->nsm, st,
-                       o.wait_polls);
+                       o.wait_polls, r.have_store ? &tsd : nullptr);
         CK(cudaGetLastError());
         if (stats) cudaEventRecord(h->ev[5], st);
         CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));

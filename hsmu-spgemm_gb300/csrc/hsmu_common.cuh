@@ -60,6 +60,8 @@ struct Window {
     int cnt;   // number of slots
     int t0;    // tile id of the first slot's column
     int redo;  // 1 when emitted by the redo pass of the learned path
+    int li;    // rows with a tile list: the window's first tile in the tile store, else -1
+    int nt;    // rows with a tile list: tiles of the window (set with cnt before the value pass)
 };
 
 // warp-class rows with at most this many entries get their values in the
@@ -208,6 +210,22 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// the same for two copies completing one barrier phase
+__device__ __forceinline__ void bulk_g2s2(void *dst1, const void *src1, unsigned bytes1, void *dst2, const void *src2,
+                                          unsigned bytes2, unsigned long long *bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes1 + bytes2)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst1)),
+                 "l"(src1), "r"(bytes1), "r"(smem_u32(bar))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst2)),
+                 "l"(src2), "r"(bytes2), "r"(smem_u32(bar))
                  : "memory");
 }
 

@@ -151,7 +151,7 @@ struct WinCursors {
 void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
                     const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st,
-                    int wait_polls = 0);
+                    int wait_polls = 0, const TileStore *ts = nullptr);
 
 int run_dmul_selftest(unsigned long long n, unsigned long long seed, unsigned long long *out, cudaStream_t st);
 // FP64 lane operations per second of a full-grid chain probe

@@ -66,9 +66,11 @@ static_assert(WIN_CAP * 8 >= (WIN_CAP + 8) * 4, "column stage fits in the accumu
 // the windows' offsets in the cursor array.  A window written with a slot
 // count of 0 (the large rows built from their stored tiles) gets its count
 // here: up to the next window's first slot when that window continues the
-// same row, else up to the row's end.
+// same row, else up to the row's end; and its tile count likewise, up to the
+// next window's first tile or the end of the row's list.
 __global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int win_cap, int M, const int *__restrict__ arp,
-                                                 const int *__restrict__ crp, Ctl *ctl, int *__restrict__ len) {
+                                                 const int *__restrict__ crp, const long long *__restrict__ ts_off,
+                                                 const int *__restrict__ ts_cnt, Ctl *ctl, int *__restrict__ len) {
     const int nwin = min(ctl->win_count, win_cap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < win_cap; w += gridDim.x * blockDim.x) {
         int n = 0;
@@ -81,10 +83,16 @@ __global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int w
             }
             n = arp[row + 1] - arp[row];
             if (win[w].cnt == 0) {
-                const int s0 = win[w].s0;
+                const int s0 = win[w].s0, li = win[w].li;
                 int e = crp[row + 1] - crp[row];
-                if (w + 1 < nwin && win[w + 1].row == row && win[w + 1].s0 > s0) e = win[w + 1].s0;
+                long long le = (li >= 0 && ts_off) ? ts_off[row] + ts_cnt[row] : -1;
+                if (w + 1 < nwin && win[w + 1].row == row && win[w + 1].s0 > s0) {
+                    e = win[w + 1].s0;
+                    if (win[w + 1].li > li) le = win[w + 1].li;
+                }
                 win[w].cnt = e - s0;
+                // the tile path of the value pass needs 1..WIN_TCAP tiles; else the columns are used
+                win[w].nt = (li >= 0 && le > li && le - li <= WIN_TCAP) ? (int)(le - li) : 0;
             }
         }
         len[w] = n;
@@ -141,7 +149,8 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                                                             const long long *__restrict__ soff,
                                                             const long long *__restrict__ woff,
                                                             const int *__restrict__ wcur, int wait_polls, int M,
-                                                            Ctl *ctl) {
+                                                            const int *__restrict__ ts_tcol,
+                                                            const TileEnt *__restrict__ ts_tent, Ctl *ctl) {
     extern __shared__ __align__(16) unsigned long long s_dyn[];
     const int lane = lane_id(), w = threadIdx.x >> 5;
     NumSmem &S = reinterpret_cast<NumSmem *>(s_dyn)[w];
@@ -173,17 +182,33 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 bad = true;
                 continue;
             }
-            // columns of the window: in C, or (learned path, speculative pass) still in the row's
-            // slot -- then they are copied to C here while the table is built.  One bulk copy
-            // brings them into the accumulator's space (16-byte aligned: `head` ints before)
+            // The window's tile table comes from one of two sources.  Rows with a tile
+            // list (the count pass kept their C tiles): the window's tiles themselves -- id,
+            // mask and first slot -- so the table is filled with one store per tile.  Other
+            // rows: the window's sorted columns, in C or (learned path, speculative pass)
+            // still in the row's slot -- then they are copied to C here while the table is
+            // built.  Either way bulk copies bring them into the accumulator's space.
             const bool from_slot = scol != nullptr && !W.redo;
-            const int *__restrict__ gsrc = from_slot ? scol + soff[row] + W.s0 : ccol + s0;
-            const uintptr_t ga = reinterpret_cast<uintptr_t>(gsrc);
-            const int lead = (int)((ga & 15u) >> 2);
-            const unsigned bytes = (unsigned)(((lead + cnt) * 4 + 15) & ~15);
+            const bool tiles_in = ts_tent != nullptr && W.li >= 0 && W.nt > 0 && !from_slot;
+            const int nt = W.nt;
             int *stage = reinterpret_cast<int *>(S.acc);
+            int lead = 0;
             __syncwarp();
-            if (lane == 0) bulk_g2s(stage, reinterpret_cast<const void *>(ga & ~(uintptr_t)15), bytes, &S.bar);
+            if (tiles_in) {
+                // entries (16 bytes each) at the start of the stage, tile ids 4096 bytes in
+                const uintptr_t ga = reinterpret_cast<uintptr_t>(ts_tcol + W.li);
+                lead = (int)((ga & 15u) >> 2);
+                const unsigned bytes_c = (unsigned)(((lead + nt) * 4 + 15) & ~15);
+                if (lane == 0)
+                    bulk_g2s2(stage, ts_tent + W.li, (unsigned)nt * 16u, stage + 1024,
+                              reinterpret_cast<const void *>(ga & ~(uintptr_t)15), bytes_c, &S.bar);
+            } else {
+                const int *__restrict__ gsrc = from_slot ? scol + soff[row] + W.s0 : ccol + s0;
+                const uintptr_t ga = reinterpret_cast<uintptr_t>(gsrc);
+                lead = (int)((ga & 15u) >> 2);
+                const unsigned bytes = (unsigned)(((lead + cnt) * 4 + 15) & ~15);
+                if (lane == 0) bulk_g2s(stage, reinterpret_cast<const void *>(ga & ~(uintptr_t)15), bytes, &S.bar);
+            }
             for (int q = lane; q < WIN_TCAP; q += WARP) S.tmask[q] = 0ull;
             for (int q = lane; q < WIN_OCCW; q += WARP) S.occ[q] = 0ull;
             // wait_polls > 0 (a test hook): that many non-blocking polls, then give up
@@ -198,8 +223,18 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
                 return;
             }
             phase ^= 1u;
-            const int *src = stage + lead;
-            const int c_lo = src[0], c_hi = src[cnt - 1];
+            const int *src = stage + lead;  // the columns (column path)
+            const TileEnt *ent = reinterpret_cast<const TileEnt *>(stage);  // the tiles (tile path)
+            const int *tid = stage + 1024 + lead;
+            int c_lo, c_hi;
+            if (tiles_in) {
+                const unsigned long long m_last = ent[nt - 1].mask;
+                c_lo = (tid[0] << 6) + (ent[0].mask ? __ffsll((long long)ent[0].mask) - 1 : 0);
+                c_hi = (tid[nt - 1] << 6) + (m_last ? 63 - __clzll((long long)m_last) : 0);
+            } else {
+                c_lo = src[0];
+                c_hi = src[cnt - 1];
+            }
             const int span = (c_hi >> 6) - t0 + 1;
             if (span <= 0 || span > WIN_SPAN || (c_lo >> 6) != t0) {
                 bad = true;
@@ -216,12 +251,31 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
             const int *__restrict__ cur0 = wcur + woff[wi];
             const int *__restrict__ cur1 = cont ? wcur + woff[wi + 1] : nullptr;
 
-            // ---- tile table from the window's sorted columns.  dense: span <= WIN_TCAP,
-            // tmask/tbase indexed by tile - t0; otherwise two-level (occupancy + rank).
+            // ---- tile table.  dense: span <= WIN_TCAP, tmask/tbase indexed by tile - t0;
+            // otherwise two-level (occupancy + rank).
             const bool dense = span <= WIN_TCAP;
             const int nwords = (span + 63) >> 6;
             __syncwarp();
-            if (dense) {
+            if (tiles_in) {
+                // one store per tile: its mask and its first slot (row-relative in the list,
+                // window-relative here); a two-level table numbers the tiles by rank
+                int ent_sum = 0;
+                for (int q = lane; q < nt; q += WARP) {
+                    const int t = tid[q] - t0;
+                    const unsigned long long m = ent[q].mask;
+                    const int slot = (int)(unsigned)ent[q].info - W.s0;
+                    ent_sum += popc64(m);
+                    if ((unsigned)t >= (unsigned)span || (unsigned)slot >= (unsigned)cnt) {
+                        bad = true;
+                    } else {
+                        const int r = dense ? t : q;
+                        S.tmask[r] = m;
+                        S.tbase[r] = (unsigned short)slot;
+                        if (!dense) smem_setbit64(&S.occ[t >> 6], t & 63);
+                    }
+                }
+                if (warp_sum(ent_sum) != cnt) bad = true;
+            } else             if (dense) {
                 // dense: the window's column bitmap (one 32-bit shared atomic per column),
                 // then every tile's first slot as the count of columns in the tiles before it
                 for (int sb = 0; sb < cnt; sb += WARP) {
@@ -339,17 +393,18 @@ __global__ void __launch_bounds__(NUM_WARPS * 32, NUM_CTAS_PER_SM) k_numeric(con
 void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const int *crp, int *ccol, double *cval,
                     const Window *win, long long win_cap, const unsigned char *flag, const int *scol,
                     const long long *soff, const WinCursors &wc, Ctl *ctl, int arith, int nsm, cudaStream_t st,
-                    int wait_polls) {
+                    int wait_polls, const TileStore *ts) {
     if (win_cap <= 0) return;
     cudaMemsetAsync(&ctl->win_next, 0, sizeof(int), st);
-    k_win_len<<<nsm * 4, 256, 0, st>>>(const_cast<Window *>(win), (int)win_cap, A.M, A.rp, crp, ctl, wc.len);
+    k_win_len<<<nsm * 4, 256, 0, st>>>(const_cast<Window *>(win), (int)win_cap, A.M, A.rp, crp, ts ? ts->off : nullptr,
+                                       ts ? ts->cnt : nullptr, ctl, wc.len);
     launch_scan64(wc.len, wc.off, (int)win_cap, wc.total, wc.scan_tmp, st);
     k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, A.M, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
                                             Bt.off, wc.cur, ctl);
     auto k = arith == AR_IMUL ? k_numeric<AR_IMUL> : arith == AR_FMA ? k_numeric<AR_FMA> : k_numeric<AR_RN>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
         A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, wc.off, wc.cur,
-        wait_polls, A.M, ctl);
+        wait_polls, A.M, ts ? ts->tcol : nullptr, ts ? ts->tent : nullptr, ctl);
 }
 
 int configure_numeric() {

@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(SDS_WARPS * 32, SDS_CTAS_PER_SM)
             for (int j = lane; j < nwin; j += WARP) {
                 const int s0 = S.wl[j];
                 const int e = (j + 1 < nwin) ? S.wl[j + 1] : total;
-                win[wbase + j] = Window{i, s0, e - s0, t0 + S.wt[j], out.mode == OUT_REDO};
+                win[wbase + j] = Window{i, s0, e - s0, t0 + S.wt[j], out.mode == OUT_REDO, -1, 0};
             }
         }
         emit_tiles(S.msk, S.base, lo, hi, t0 << 6, ccol + rowbase);
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__
                 for (int j = threadIdx.x; j < nwin; j += SL_THREADS) {
                     const int s0 = S.wl[j];
                     const int e = (j + 1 < nwin) ? S.wl[j + 1] : chunk_end;
-                    win[wbase + j] = Window{i, s0, e - s0, c0 + S.wt[j], out.mode == OUT_REDO};
+                    win[wbase + j] = Window{i, s0, e - s0, c0 + S.wt[j], out.mode == OUT_REDO, -1, 0};
                 }
                 block_emit_tiles(S.msk, S.base, len, w, NWARP, c0 << 6, ccol + rowbase);
             }
@@ -452,7 +452,8 @@ __global__ void __launch_bounds__(SLS_THREADS, 6) k_struct_ls(int M, RowInfo ri,
                 const int slot = (int)(unsigned)info;
                 const int ord1 = (int)(info >> 32);
                 if (ord1) {
-                    if (ord1 <= nwin) win[wbase + ord1 - 1] = Window{i, slot, 0, t, out.mode == OUT_REDO};
+                    if (ord1 <= nwin)
+                        win[wbase + ord1 - 1] = Window{i, slot, 0, t, out.mode == OUT_REDO, (int)(sb + q), 0};
                     else set_err(&ctl->err, DERR_INTERNAL);
                 }
                 // the 32 tiles' entries: slots s0 .. s0 + (their entries) - 1 of the row
