@@ -58,6 +58,9 @@ struct hsmu_handle_s {
     // host-buffer entry: copy streams and their ordering events
     cudaStream_t cs_in, cs_out;
     cudaEvent_t ev_in, ev_panel, ev_out;
+    // B's tile conversion runs on its own stream beside the bounds pass
+    cudaStream_t cs_tiles;
+    cudaEvent_t ev_tiles_start, ev_tiles_done;
 };
 
 namespace {
@@ -84,6 +87,9 @@ const char *kErr[] = {"ok",
 // last panel, and its sizes shrink by HOST_PANEL_RATIO from the first (small
 // panels leave the GPU partly idle, so only one end is made small).
 constexpr long long HOST_PANEL_BYTES = 32ll << 20;
+
+// entries of B from which its tile conversion runs on a second stream beside the bounds pass
+constexpr int TILES_ASIDE_MIN_NNZ = 1 << 19;
 constexpr long long HOST_MAX_PANELS = 8;
 constexpr double HOST_PANEL_GROWTH = 2.0;
 constexpr double HOST_PANEL_RATIO = 0.7;
@@ -164,9 +170,15 @@ void free_owned(std::initializer_list<const void *> ptrs) {
 }
 
 // B -> tiles into caller-visible arrays (tile arrays sized by nnz(B) >= tiles)
+// B -> 64-column tiles.  Allocations on `st`; with `run` the kernels run on that
+// stream instead (after everything already queued on `st`), the scratch is
+// released there too, and ev_done marks the end: the caller makes `st` wait on
+// it before anything reads the tiles.
 int build_tiles(hsmu_handle_s *h, const hsmu_csr *B, hsmu_btiles *out, Ctl *ctl, int validate, cudaStream_t st,
-                bool read_count) {
+                bool read_count, cudaStream_t run = nullptr, cudaEvent_t ev_start = nullptr,
+                cudaEvent_t ev_done = nullptr) {
     int rc = HSMU_OK;
+    cudaStream_t ks = st;
     int *tcnt = nullptr, *scan_tmp = nullptr;
     long long *tot = nullptr;
     DevCSR Bd = dev(B);
@@ -184,17 +196,23 @@ int build_tiles(hsmu_handle_s *h, const hsmu_csr *B, hsmu_btiles *out, Ctl *ctl,
     CK(palloc(&tcnt, (size_t)B->M + 1, st));
     CK(palloc(&scan_tmp, scan_tmp_ints(B->M), st));
     CK(palloc(&tot, 1, st));
-    launch_tiles_count(Bd, tcnt, validate, ctl, grid_rows(h), st);
-    launch_scan(tcnt, out->tile_ptr, B->M, tot, scan_tmp, ctl, st);
-    launch_tiles_fill(Bd, out->tile_ptr, out->tile_col, reinterpret_cast<unsigned long long *>(out->mask), out->tile_off, ctl, grid_rows(h), st);
+    if (run && ev_start && ev_done) {
+        CK(cudaEventRecord(ev_start, st));
+        CK(cudaStreamWaitEvent(run, ev_start, 0));
+        ks = run;
+    }
+    launch_tiles_count(Bd, tcnt, validate, ctl, grid_rows(h), ks);
+    launch_scan(tcnt, out->tile_ptr, B->M, tot, scan_tmp, ctl, ks);
+    launch_tiles_fill(Bd, out->tile_ptr, out->tile_col, reinterpret_cast<unsigned long long *>(out->mask), out->tile_off, ctl, grid_rows(h), ks);
     CK(cudaGetLastError());
     if (read_count) {
-        CK(cudaMemcpyAsync(&ctl->ntiles, out->tile_ptr + B->M, sizeof(int), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(&ctl->ntiles, out->tile_ptr + B->M, sizeof(int), cudaMemcpyDeviceToDevice, ks));
     }
 done:
-    pfree(tcnt, st);
-    pfree(scan_tmp, st);
-    pfree(tot, st);
+    pfree(tcnt, ks);
+    pfree(scan_tmp, ks);
+    pfree(tot, ks);
+    if (ks != st && ev_done) cudaEventRecord(ev_done, ks);
     if (rc != HSMU_OK) {
         // stream-ordered allocations go back the same way
         pfree(out->tile_ptr, st);
@@ -227,6 +245,7 @@ struct PlainRun {
     DevCSR Ad{}, Bd{};
     hsmu_btiles bt{};
     bool own_tiles = false;
+    bool tiles_aside = false;  // B's tiles are being built on the handle's conversion stream
     DevTiles Btd{};
     RowInfo ri{};
     int *scan_tmp = nullptr;
@@ -290,13 +309,21 @@ struct PlainRun {
         if (Bt_in) {
             bt = *Bt_in;
         } else {
-            const int rc = build_tiles(h, B, &bt, ctl, 0, st, count_tiles);
-            if (rc) return rc;
+            // B's tiles on their own stream, beside the bounds pass (which reads B's columns);
+            // a small B is converted in line (the hand-over would cost more than it overlaps)
+            tiles_aside = B->nnz >= TILES_ASIDE_MIN_NNZ;
+            const int rc = tiles_aside ? build_tiles(h, B, &bt, ctl, 0, st, count_tiles, h->cs_tiles,
+                                                     h->ev_tiles_start, h->ev_tiles_done)
+                                       : build_tiles(h, B, &bt, ctl, 0, st, count_tiles);
+            if (rc) {
+                if (tiles_aside) cudaStreamWaitEvent(st, h->ev_tiles_done, 0);
+                return rc;
+            }
             own_tiles = true;
             launches += 5;
         }
         Btd = DevTiles{bt.tile_ptr, bt.tile_col, reinterpret_cast<const unsigned long long *>(bt.mask), bt.tile_off};
-        if (ev_tiles) cudaEventRecord(ev_tiles, st);
+        if (ev_tiles) cudaEventRecord(ev_tiles, tiles_aside ? h->cs_tiles : st);
         CKR(palloc(&ri.prod, (size_t)M, st));
         CKR(palloc(&ri.tmin, (size_t)M, st));
         CKR(palloc(&ri.tmax, (size_t)M, st));
@@ -307,7 +334,7 @@ struct PlainRun {
         CKR(palloc(&scan_tmp, scan_tmp_ints(M), st));
         if (store) {
             CKR(grow_arena());
-            CKR(palloc(&ri.tcap, (size_t)M, st));
+            ri.store = 1;
             if (h->arena_cap > 0) {
                 CKR(palloc(&ts_off, (size_t)M, st));
                 CKR(palloc(&ts_cnt, (size_t)M, st));
@@ -317,8 +344,10 @@ struct PlainRun {
                 have_store = true;
             }
         }
-        launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
+        launch_bounds(Ad, Bd, ri, ctl, grid_rows(h), scan_tmp, st);
         launches += 6;  // bounds + binning
+        // everything after this reads B's tiles
+        if (tiles_aside) CKR(cudaStreamWaitEvent(st, h->ev_tiles_done, 0));
         CKR(cudaGetLastError());
         return HSMU_OK;
     }
@@ -363,7 +392,7 @@ struct PlainRun {
         if (host_rp) CKR(cudaMemcpyAsync(host_rp, crp, sizeof(int32_t) * ((size_t)M + 1), cudaMemcpyDeviceToHost, st));
         CKR(cudaStreamSynchronize(st));
         hc = *h->h_ctl;
-        if (ri.tcap && hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;  // for the next call
+        if (ri.store && hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;  // for the next call
         if (hc.err) return err_from_dev(hc.err);
         if (hc.nnz > INT_MAX) return HSMU_ERR_OVERFLOW;
         win_cap = (long long)hc.win_bound;
@@ -451,7 +480,6 @@ struct PlainRun {
         pfree(ri.cls, st);
         pfree(ri.bin_cnt, st);
         pfree(ri.cnnz, st);
-        pfree(ri.tcap, st);
         pfree(ts_off, st);
         pfree(ts_cnt, st);
         pfree(ts_nwin, st);
@@ -737,9 +765,10 @@ int spgemm_learned_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, 
         (hc.products == 0 || (double)hc.wide_ds_prod < LEARNED_MIN_SHARE * (double)hc.products))
         goto plain;
     {
-        // the large rows' tile lists: the arena is sized now, from the bounds pass's need
-        if (r.ri.tcap && hc.bin_count[BIN_L] > 0) {
-            if (hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;
+        // the large rows' tile lists: the arena is sized now, from what earlier calls needed
+        // or else from the bounds pass's bound (the sum of the large rows' tile spans)
+        if (r.ri.store && hc.bin_count[BIN_L] > 0) {
+            if (h->arena_want == 0) h->arena_want = hc.span_tiles;
             CK(r.grow_arena());
             if (h->arena_cap > 0 && !r.ts_off) {
                 CK(palloc(&r.ts_off, (size_t)M, st));
@@ -863,6 +892,7 @@ learned:
             rc = err_from_dev(hc.err);
             goto done;
         }
+        if (r.ri.store && hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;  // for the next call
         if (hc.nnz > INT_MAX) {
             rc = HSMU_ERR_OVERFLOW;
             goto done;
@@ -968,7 +998,7 @@ int row_nnz_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, int32_t
     CK(palloc(&ri.bin_cnt, bin_scratch_ints(M), st));
     CK(palloc(&scan_tmp, scan_tmp_ints(M), st));
     ri.cnnz = nnz_out;
-    launch_bounds(Ad, Bd, Btd, ri, ctl, grid_rows(h), scan_tmp, st);
+    launch_bounds(Ad, Bd, ri, ctl, grid_rows(h), scan_tmp, st);
     launch_count(Ad, Bd, Btd, ri, ctl, h->nsm, st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -1117,7 +1147,10 @@ int hsmu_handle_create(hsmu_handle *out) {
         cudaStreamCreateWithFlags(&h->cs_out, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->cs_tiles, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_tiles_start, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_tiles_done, cudaEventDisableTiming) != cudaSuccess) {
         hsmu_handle_destroy(h);
         return HSMU_ERR_CUDA;
     }
@@ -1142,7 +1175,7 @@ int hsmu_handle_destroy(hsmu_handle h) {
     if (!h) return HSMU_OK;
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out})
+    for (cudaEvent_t e : {h->ev_in, h->ev_panel, h->ev_out, h->ev_tiles_start, h->ev_tiles_done})
         if (e) cudaEventDestroy(e);
     if (h->arena_col || h->arena_ent) {
         cudaDeviceSynchronize();  // no call of this handle still reads the arena
@@ -1150,7 +1183,7 @@ int hsmu_handle_destroy(hsmu_handle h) {
             if (p) cudaFreeAsync(p, 0);
         cudaStreamSynchronize(0);
     }
-    for (cudaStream_t s : {h->cs_in, h->cs_out})
+    for (cudaStream_t s : {h->cs_in, h->cs_out, h->cs_tiles})
         if (s) cudaStreamDestroy(s);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
     delete h;

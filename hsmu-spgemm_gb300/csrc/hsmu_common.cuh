@@ -84,7 +84,8 @@ struct Ctl {
                                      // rows (bounds pass) + warp rows above FUSE_CAP (count pass)
     unsigned long long cur_bound_ds; // same for every warp row with more than FUSE_CAP products
                                      // (bounds pass; for paths without a count pass)
-    long long store_tiles;           // sum of RowInfo::tcap: arena entries the large rows could use
+    long long store_tiles;           // arena entries the large rows' lists may take (count pass)
+    long long span_tiles;            // sum of the large rows' tile spans (bounds pass): a bound on it
     long long store_used;            // arena entries reserved by the count pass
     unsigned long long wide_ds_prod; // products of warp-class rows with more than FUSE_CAP products
     unsigned long long pred_wide_prod;  // learned path: products of warp-class rows predicted

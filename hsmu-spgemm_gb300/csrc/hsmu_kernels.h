@@ -48,15 +48,16 @@ struct RowInfo {
     signed char *cls;  // row class (RowBin) of every row, -1 for an empty row
     int *bin_cnt;      // [NBIN][ceil(M/32)] rows of each class per 32-row chunk, then
                        // its exclusive scan (bin_scratch_ints(M) entries)
-    int *tcap;         // nullable: C tiles a large-class row can have, min(tile span, sum of
-                       // its B rows' tile counts); 0 for the other rows (bounds pass)
+    int store;         // 1: the tile store is in use -- the count pass sizes each large row's
+                       // list, min(tile span, sum of its B rows' tile counts), and adds the
+                       // sizes up in Ctl::store_tiles (the arena the next call wants)
 };
 
 // C tiles of the large-class rows, kept by the count pass (which builds them
 // anyway) so that the structure pass streams each row's tile list instead of
-// repeating the OR walk over B's tiles.  Each large row reserves RowInfo::tcap
-// entries of the arena (tcol/tent, `cap` entries, owned by the handle) with
-// one atomic; a row that finds the arena full keeps nothing (cnt[i] = -1) and
+// repeating the OR walk over B's tiles.  Each large row reserves min(tile span,
+// sum of its B rows' tile counts) entries of the arena (tcol/tent, `cap`
+// entries, owned by the handle) with one atomic; a row that finds the arena full keeps nothing (cnt[i] = -1) and
 // the structure pass walks B for it as before.  Row i's list:
 // tcol/tent[off[i] .. off[i] + cnt[i]), tile ids ascending.
 //
@@ -90,8 +91,7 @@ void launch_tiles_fill(const DevCSR &B, const int *tptr, int *tcol, unsigned lon
 void launch_validate(const DevCSR &A, Ctl *ctl, int grid, cudaStream_t st);
 
 // k_rows.cu
-void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int grid, int *scan_tmp,
-                   cudaStream_t st);
+void launch_bounds(const DevCSR &A, const DevCSR &B, RowInfo ri, Ctl *ctl, int grid, int *scan_tmp, cudaStream_t st);
 // exclusive scan of int counts (n entries) into out[0..n]; total (int64) into *total64;
 // sets DERR_OVERFLOW if the total exceeds INT32_MAX.  tmp must hold scan_tmp_ints(n) ints.
 // in == out (an in-place scan) is allowed.

@@ -4,8 +4,9 @@
 // sum_{k in A(i,:)} nnz(B(k,:)) (64-bit; the reference counts it on the host,
 // src/NHC_spgemm.cuh:37-42, and bounds C tiles per row with k_compute_flop,
 // src/small/mask.cuh:14-51) and the exact first/last C tile of the row (the
-// min/max over the first/last tile of every referenced B row, which are at
-// the ends of B's sorted tile lists).  The tile span decides the row class
+// min/max over the 64-column tiles of every referenced B row's first and last
+// column -- read from B itself, so this pass does not wait for B's tiles and
+// runs beside their construction).  The tile span decides the row class
 // (one warp with a dense span table, or one CTA with a chunked table), which
 // replaces the reference's host-round-trip binning (src/bining.cuh:1-207):
 // rows are binned on the device by a stable compaction (count per 32-row
@@ -26,35 +27,33 @@ namespace hsmu {
 
 template <int G>
 __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ arp, const int *__restrict__ acol,
-                                                const int *__restrict__ brp, const int *__restrict__ tptr,
-                                                const int *__restrict__ tcol, int N, RowInfo ri, Ctl *ctl) {
+                                                const int *__restrict__ brp, const int *__restrict__ bcol, int N,
+                                                RowInfo ri, Ctl *ctl) {
     constexpr int RPB = 256 / G;  // rows per block iteration
     __shared__ int s_cnt[NBIN];
     const int sub = threadIdx.x & (G - 1);
     const int rloc = threadIdx.x / G;
-    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0, my_tc = 0, my_wdp = 0;
+    unsigned long long my_prod = 0, my_wb = 0, my_cb = 0, my_cbd = 0, my_wdp = 0, my_span = 0;
     if (threadIdx.x < NBIN) s_cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int rb = blockIdx.x * RPB; rb < M; rb += gridDim.x * RPB) {
         const int i = rb + rloc;
-        long long prod = 0, tsum = 0;
+        long long prod = 0;
         int tmin = INT_MAX, tmax = -1;
         if (i < M) {
             for (int p = arp[i] + sub; p < arp[i + 1]; p += G) {
                 const int k = __ldg(acol + p);
-                prod += __ldg(brp + k + 1) - __ldg(brp + k);
-                const int t0 = __ldg(tptr + k), t1 = __ldg(tptr + k + 1);
-                tsum += t1 - t0;
-                if (t1 > t0) {
-                    tmin = min(tmin, __ldg(tcol + t0));
-                    tmax = max(tmax, __ldg(tcol + t1 - 1));
+                const int bs = __ldg(brp + k), be = __ldg(brp + k + 1);
+                prod += be - bs;
+                if (be > bs) {
+                    tmin = min(tmin, __ldg(bcol + bs) >> 6);
+                    tmax = max(tmax, __ldg(bcol + be - 1) >> 6);
                 }
             }
         }
 #pragma unroll
         for (int d = G / 2; d > 0; d >>= 1) {
             prod += __shfl_xor_sync(FULL, prod, d, G);
-            tsum += __shfl_xor_sync(FULL, tsum, d, G);
             tmin = min(tmin, __shfl_xor_sync(FULL, tmin, d, G));
             tmax = max(tmax, __shfl_xor_sync(FULL, tmax, d, G));
         }
@@ -76,20 +75,16 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
                 const unsigned long long wb = (unsigned long long)(cap / WIN_CUT + tl / WIN_TCAP + (span - 1) / WIN_SPAN + 1);
                 my_wb += wb;
                 // rows that can reach the window pass: the large class, and warp rows above FUSE_CAP
-                if (bin == BIN_L) my_cb += wb * (unsigned long long)(arp[i + 1] - arp[i]);
+                if (bin == BIN_L) {
+                    my_cb += wb * (unsigned long long)(arp[i + 1] - arp[i]);
+                    my_span += (unsigned long long)span;
+                }
                 if (bin == BIN_DS && prod > FUSE_CAP) {
                     my_cbd += wb * (unsigned long long)(arp[i + 1] - arp[i]);
                     my_wdp += (unsigned long long)prod;
                 }
             }
             ri.cls[i] = (signed char)bin;
-            if (ri.tcap) {
-                // a large row has at most one C tile per tile of its span and per B tile it reads
-                const long long span = prod ? (long long)(tmax - tmin + 1) : 0;
-                const int tc = bin == BIN_L ? (int)(tsum < span ? tsum : span) : 0;
-                ri.tcap[i] = tc;
-                my_tc += (unsigned long long)tc;
-            }
         }
     }
     __syncthreads();
@@ -98,11 +93,11 @@ __global__ void __launch_bounds__(256) k_bounds(int M, const int *__restrict__ a
     my_wb = warp_sum(my_wb);
     my_cb = warp_sum(my_cb);
     my_cbd = warp_sum(my_cbd);
-    my_tc = warp_sum(my_tc);
     my_wdp = warp_sum(my_wdp);
+    my_span = warp_sum(my_span);
     if (lane_id() == 0) {
         if (my_wdp) atomicAdd(&ctl->wide_ds_prod, my_wdp);
-        if (my_tc) atomicAdd(reinterpret_cast<unsigned long long *>(&ctl->store_tiles), my_tc);
+        if (my_span) atomicAdd(reinterpret_cast<unsigned long long *>(&ctl->span_tiles), my_span);
         if (my_prod) atomicAdd(&ctl->products, my_prod);
         if (my_wb) atomicAdd(&ctl->win_bound, my_wb);
         if (my_cb) atomicAdd(&ctl->cur_bound, my_cb);
@@ -143,17 +138,16 @@ __global__ void __launch_bounds__(256) k_bin_emit(int M, const signed char *__re
 
 size_t bin_scratch_ints(int M) { return (size_t)NBIN * ((M + WARP - 1) / WARP) * 2 + 2; }
 
-void launch_bounds(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowInfo ri, Ctl *ctl, int grid,
-                   int *scan_tmp, cudaStream_t st) {
+void launch_bounds(const DevCSR &A, const DevCSR &B, RowInfo ri, Ctl *ctl, int grid, int *scan_tmp, cudaStream_t st) {
     const double avg = A.M ? (double)A.nnz / A.M : 0.0;
     if (avg <= 6)
-        k_bounds<4><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+        k_bounds<4><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, B.N, ri, ctl);
     else if (avg <= 12)
-        k_bounds<8><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+        k_bounds<8><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, B.N, ri, ctl);
     else if (avg <= 24)
-        k_bounds<16><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+        k_bounds<16><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, B.N, ri, ctl);
     else
-        k_bounds<32><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, Bt.ptr, Bt.col, B.N, ri, ctl);
+        k_bounds<32><<<grid, 256, 0, st>>>(A.M, A.rp, A.col, B.rp, B.col, B.N, ri, ctl);
     const int nch = (A.M + WARP - 1) / WARP;
     int *cnt = ri.bin_cnt, *off = ri.bin_cnt + (size_t)NBIN * nch + 1;
     k_bin_count<<<grid, 256, 0, st>>>(A.M, ri.cls, cnt);

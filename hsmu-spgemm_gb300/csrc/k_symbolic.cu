@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
     extern __shared__ unsigned long long s_dyn[];
     unsigned long long *msk = s_dyn;  // DCH_COUNT entries
     __shared__ int s_red[L_THREADS / 32];
+    __shared__ long long s_tsum[L_THREADS / 32];
     __shared__ ListSmem<L_THREADS / 32> s_ls;
     __shared__ long long s_off;
     const int lane = lane_id(), w = threadIdx.x >> 5;
@@ -108,7 +109,23 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
         int total = 0;
         ListRun run{0, 0, 0, -1ll};
         long long sbase = -1;
-        const int scap = STORE ? ri.tcap[i] : 0;
+        int scap = 0;
+        if (ri.store) {
+            // the row's list has at most one C tile per tile of its span and per B tile it
+            // reads; the sizes add up to the arena the next call wants
+            long long ts_sum = 0;
+            for (int p = a_lo + (int)threadIdx.x; p < a_hi; p += L_THREADS) {
+                const int k = __ldg(acol + p);
+                ts_sum += __ldg(tptr + k + 1) - __ldg(tptr + k);
+            }
+            ts_sum = warp_sum(ts_sum);
+            if (lane == 0) s_tsum[w] = ts_sum;
+            __syncthreads();
+            long long tsum = 0;
+            for (int j = 0; j < NWARP; j++) tsum += s_tsum[j];
+            scap = (int)min(tsum, (long long)(tmax - tmin + 1));
+            if (threadIdx.x == 0) atomicAdd(reinterpret_cast<unsigned long long *>(&ctl->store_tiles), (unsigned long long)scap);
+        }
         if (STORE) {
             // reserve the row's list in the arena (none when it is full)
             if (threadIdx.x == 0) {
@@ -194,7 +211,7 @@ void launch_count_small(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, Ro
 void launch_count_large(const DevCSR &A, const DevTiles &Bt, RowInfo ri, const TileStore *ts, Ctl *ctl, int nsm,
                         cudaStream_t st) {
     const size_t smem = DCH_COUNT * sizeof(unsigned long long);
-    if (ts && ts->tcol && ts->tent && ts->cap > 0 && ri.tcap)
+    if (ts && ts->tcol && ts->tent && ts->cap > 0 && ri.store)
         k_count_l<LM_STORE><<<nsm * 6, L_THREADS, smem, st>>>(A.M, A.rp, A.col, Bt.ptr, Bt.col, Bt.mask, ri, *ts,
                                                                RowOut{}, ctl);
     else
