@@ -158,13 +158,17 @@ __device__ bool chunk_to_list(const unsigned long long *msk, int len, int c0, in
 
 // Columns of 32 consecutive tiles of a row's list, one per lane (t, m; lanes
 // past the list carry m = 0), whose first entry goes to out[0].  The tiles'
-// entries are consecutive in the row, so every store of the warp lands in
-// one contiguous run:
+// entries are consecutive in the row:
 //   dense tiles (at least EMIT_DENSE entries on average): one tile at a time,
-//     lane b writes the entries of bits b and b + 32;
-//   sparse tiles: lane k of each step writes entry kb + k, found as the
+//     lane b writes the entries of bits b and b + 32 (every store of the warp
+//     lands in one contiguous run);
+//   sparse tiles, none with more than EMIT_OWN entries: every lane writes its
+//     own tile's entries, lowest set bit first (as many steps as the fullest
+//     tile has entries; the stores of a step land a few entries apart);
+//   otherwise: lane k of each step writes entry kb + k, found as the
 //     (k - first entry of its tile)-th set bit of its tile's mask.
 constexpr int EMIT_DENSE = 10;
+constexpr int EMIT_OWN = 8;
 
 __device__ __forceinline__ void warp_emit_list(int t, unsigned long long m, int *__restrict__ out) {
     const int lane = lane_id();
@@ -172,6 +176,19 @@ __device__ __forceinline__ void warp_emit_list(int t, unsigned long long m, int 
     const int incl = warp_incl_scan(pc);
     const int total = __shfl_sync(FULL, incl, WARP - 1);
     const int excl = incl - pc;
+    const int most = (int)__reduce_max_sync(FULL, (unsigned)pc);
+    if (most <= EMIT_OWN) {
+        unsigned long long mm = m;
+        const int cb = t << 6;
+        int pos = excl;
+        for (int it = 0; it < most; it++) {
+            if (mm) {
+                out[pos++] = cb + __ffsll((long long)mm) - 1;
+                mm &= mm - 1ull;
+            }
+        }
+        return;
+    }
     if (total >= WARP * EMIT_DENSE) {
         const unsigned below = lanemask_lt();
         for (int j = 0; j < WARP; j++) {
