@@ -68,6 +68,18 @@ struct Window {
 // fused structure kernel; wider ones go through numeric windows
 constexpr int FUSE_CAP = 512;
 
+// Row hand-out of a kernel that gives each CTA one row at a time: a CTA starts
+// on row first + blockIdx.x and thread 0 draws its next one from `next` while
+// the current row runs.  Costs of the large rows spread over orders of
+// magnitude, so a fixed stride leaves a few CTAs running long after the rest.
+// The pair resets itself (the last CTA to run out of rows zeroes it), so
+// consecutive launches on one stream -- row panels -- need no reset between.
+struct RowCounter {
+    int next;
+    int done;
+};
+enum RowCounterId : int { ROWS_COUNT_L = 0, ROWS_STRUCT_LS = 1, ROWS_STRUCT_L = 2 };
+
 struct Ctl {
     unsigned long long products;     // sum of intermediate products
     unsigned long long win_bound;    // upper bound on the number of windows
@@ -91,6 +103,7 @@ struct Ctl {
     unsigned long long pred_wide_prod;  // learned path: products of warp-class rows predicted
                                      // above FUSE_CAP entries
     long long win_listed;            // windows of the rows with a tile list (scan total)
+    RowCounter rows[3];              // row hand-out of the kernels that give a CTA one row at a time
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -100,6 +113,29 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 }
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & (WARP - 1); }
+
+// thread 0: the CTA's next row (first: the launch's first row)
+__device__ __forceinline__ int draw_row(RowCounter *c, int first) {
+    return first + (int)gridDim.x + atomicAdd(&c->next, 1);
+}
+// all threads: the CTA's next row, drawn by thread 0 when the current one is done
+// (s_slot: a shared int of the kernel's own)
+__device__ __forceinline__ int next_row_sync(RowCounter *c, int first, int *s_slot) {
+    if (threadIdx.x == 0) *s_slot = draw_row(c, first);
+    __syncthreads();
+    const int r = *s_slot;
+    __syncthreads();
+    return r;
+}
+// thread 0, once per CTA after its last draw (every CTA of the launch, also one
+// that had no row)
+__device__ __forceinline__ void rows_done(RowCounter *c) {
+    __threadfence();
+    if (atomicAdd(&c->done, 1) == (int)gridDim.x - 1) {
+        c->next = 0;
+        c->done = 0;
+    }
+}
 
 __device__ __forceinline__ unsigned lanemask_le() { return lanemask_lt() | (1u << lane_id()); }
 

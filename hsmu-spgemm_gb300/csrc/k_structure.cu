@@ -282,14 +282,15 @@ __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__
     // warp totals of the three block scans of a chunk (one array each: one barrier per scan)
     __shared__ long long s_w0[SL_THREADS / 32], s_w1[SL_THREADS / 32];
     __shared__ int s_w2[SL_THREADS / 32];
-    __shared__ int s_wbase;
+    __shared__ int s_wbase, s_next;
     constexpr int NWARP = SL_THREADS / 32;
     const int w = threadIdx.x >> 5;
     const int *rows = ri.bins + (size_t)BIN_L * M;
     int b0, b1;
     bin_slice(rows, ctl->bin_count[BIN_L], out, M, b0, b1);
     int *__restrict__ ccol = out.ccol;
-    for (int r = b0 + blockIdx.x; r < b1; r += gridDim.x) {
+    // one row at a time from a counter (RowCounter)
+    for (int r = b0 + blockIdx.x; r < b1; r = next_row_sync(&ctl->rows[ROWS_STRUCT_L], b0, &s_next)) {
         const int i = rows[r];
         if (skip_row(out, i) || (stored && stored[i] >= 0)) continue;
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
@@ -398,6 +399,7 @@ __global__ void __launch_bounds__(SL_THREADS, 3) k_struct_l(int M, const int *__
             }
         }
     }
+    if (threadIdx.x == 0) rows_done(&ctl->rows[ROWS_STRUCT_L]);
 }
 
 // ---- large rows from their stored C tile lists (PLAIN mode, tile store present)
@@ -416,57 +418,66 @@ constexpr int SLS_THREADS = 256;
 __global__ void __launch_bounds__(SLS_THREADS, 6) k_struct_ls(int M, RowInfo ri, TileStore ts, RowOut out,
                                                            Window *__restrict__ win, long long win_cap, Ctl *ctl) {
     constexpr int NT = SLS_THREADS;
-    __shared__ int s_wbase;
+    __shared__ int s_wbase, s_next;
     const int lane = lane_id(), w = threadIdx.x >> 5;
     const int *rows = ri.bins + (size_t)BIN_L * M;
     int b0, b1;
     bin_slice(rows, ctl->bin_count[BIN_L], out, M, b0, b1);
     int *__restrict__ ccol = out.ccol;
-    for (int r = b0 + blockIdx.x; r < b1; r += gridDim.x) {
+    // one row at a time from a counter (RowCounter)
+    for (int r = b0 + blockIdx.x; r < b1;) {
+        int next = 0;
+        if (threadIdx.x == 0) next = draw_row(&ctl->rows[ROWS_STRUCT_LS], b0);
         const int i = rows[r];
-        if (skip_row(out, i)) continue;
-        const int n = ts.cnt[i];
-        if (n < 0) continue;  // no list kept (the arena was full): k_struct_l builds this row
-        const long long sb = ts.off[i];
-        const int nwin = ts.nwin[i];
-        const long long rowbase = out.crp[i];  // PLAIN or REDO: final row pointers
-        const int nnz = out.crp[i + 1] - out.crp[i];
-        int wbase;
-        if (ts.wbase) {
-            wbase = ts.wbase[i];
-        } else {
-            if (threadIdx.x == 0) s_wbase = atomicAdd(&ctl->win_count, nwin);
-            __syncthreads();
-            wbase = s_wbase;
-        }
-        if (wbase >= 0 && (long long)wbase + nwin <= win_cap) {
-            for (int q0 = w * WARP; q0 < n; q0 += NT) {
-                const int q = q0 + lane;
-                const bool v = q < n;
-                const int t = v ? __ldg(ts.tcol + sb + q) : 0;
-                // the tile's mask and slot word: one 128-bit load
-                const ulonglong2 e = v ? __ldg(reinterpret_cast<const ulonglong2 *>(ts.tent) + sb + q)
-                                       : make_ulonglong2(0ull, 0ull);
-                const unsigned long long m = e.x;
-                const long long info = (long long)e.y;
-                const int slot = (int)(unsigned)info;
-                const int ord1 = (int)(info >> 32);
-                if (ord1) {
-                    if (ord1 <= nwin)
-                        win[wbase + ord1 - 1] = Window{i, slot, 0, t, out.mode == OUT_REDO, (int)(sb + q), 0};
-                    else set_err(&ctl->err, DERR_INTERNAL);
-                }
-                // the 32 tiles' entries: slots s0 .. s0 + (their entries) - 1 of the row
-                const int s0 = __shfl_sync(FULL, slot, 0);
-                const int total = warp_sum(popc64(m));
-                if (s0 + total <= nnz) warp_emit_list(t, m, ccol + rowbase + s0);
-                else if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
+        // -1: no list kept (the arena was full), k_struct_l builds this row
+        const int n = skip_row(out, i) ? -1 : ts.cnt[i];
+        if (n >= 0) {
+            const long long sb = ts.off[i];
+            const int nwin = ts.nwin[i];
+            const long long rowbase = out.crp[i];  // PLAIN or REDO: final row pointers
+            const int nnz = out.crp[i + 1] - out.crp[i];
+            int wbase;
+            if (ts.wbase) {
+                wbase = ts.wbase[i];
+            } else {
+                if (threadIdx.x == 0) s_wbase = atomicAdd(&ctl->win_count, nwin);
+                __syncthreads();
+                wbase = s_wbase;
             }
-        } else if (threadIdx.x == 0) {
-            set_err(&ctl->err, DERR_CAPACITY);
+            if (wbase >= 0 && (long long)wbase + nwin <= win_cap) {
+                for (int q0 = w * WARP; q0 < n; q0 += NT) {
+                    const int q = q0 + lane;
+                    const bool v = q < n;
+                    const int t = v ? __ldg(ts.tcol + sb + q) : 0;
+                    // the tile's mask and slot word: one 128-bit load
+                    const ulonglong2 e = v ? __ldg(reinterpret_cast<const ulonglong2 *>(ts.tent) + sb + q)
+                                           : make_ulonglong2(0ull, 0ull);
+                    const unsigned long long m = e.x;
+                    const long long info = (long long)e.y;
+                    const int slot = (int)(unsigned)info;
+                    const int ord1 = (int)(info >> 32);
+                    if (ord1) {
+                        if (ord1 <= nwin)
+                            win[wbase + ord1 - 1] = Window{i, slot, 0, t, out.mode == OUT_REDO, (int)(sb + q), 0};
+                        else set_err(&ctl->err, DERR_INTERNAL);
+                    }
+                    // the 32 tiles' entries: slots s0 .. s0 + (their entries) - 1 of the row
+                    const int s0 = __shfl_sync(FULL, slot, 0);
+                    const int total = warp_sum(popc64(m));
+                    if (s0 + total <= nnz) warp_emit_list(t, m, ccol + rowbase + s0);
+                    else if (lane == 0) set_err(&ctl->err, DERR_INTERNAL);
+                }
+            } else if (threadIdx.x == 0) {
+                set_err(&ctl->err, DERR_CAPACITY);
+            }
         }
-        if (!ts.wbase) __syncthreads();  // s_wbase is reused by the next row
+        // s_wbase and s_next are rewritten only after the second barrier
+        if (threadIdx.x == 0) s_next = next;
+        __syncthreads();
+        r = s_next;
+        __syncthreads();
     }
+    if (threadIdx.x == 0) rows_done(&ctl->rows[ROWS_STRUCT_LS]);
 }
 
 constexpr int TINYF_THREADS = 128;

@@ -97,11 +97,15 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
     __shared__ long long s_tsum[L_THREADS / 32];
     __shared__ ListSmem<L_THREADS / 32> s_ls;
     __shared__ long long s_off;
+    __shared__ int s_next;
     const int lane = lane_id(), w = threadIdx.x >> 5;
     constexpr int NWARP = L_THREADS / 32;
     const int n = ctl->bin_count[BIN_L];
     const int *rows = ri.bins + (size_t)BIN_L * M;
-    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+    // one row at a time from a counter (RowCounter)
+    for (int r = blockIdx.x; r < n;) {
+        int next = 0;
+        if (threadIdx.x == 0) next = draw_row(&ctl->rows[ROWS_COUNT_L], 0);
         const int i = rows[r];
         const int tmin = ri.tmin[i], tmax = ri.tmax[i];
         const int a_lo = arp[i], a_hi = arp[i + 1];
@@ -178,8 +182,13 @@ __global__ void __launch_bounds__(L_THREADS, 6) k_count_l(int M, const int *__re
                 ts.nwin[i] = listed ? run.wins : 0;   // scanned in row order into the rows' first windows
             }
             if (SPEC) out.flag[i] = listed ? ROW_OVERFLOW : ROW_NONE;  // unlisted: the OR-walk kernel
+            s_next = next;
         }
+        __syncthreads();
+        r = s_next;
+        __syncthreads();
     }
+    if (threadIdx.x == 0) rows_done(&ctl->rows[ROWS_COUNT_L]);
 }
 
 constexpr int TINY_THREADS = 256;
