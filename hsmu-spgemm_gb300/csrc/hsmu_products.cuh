@@ -253,11 +253,15 @@ __device__ __forceinline__ void warp_accumulate(int a_lo, int a_hi, const int *_
                 } else {
                     const unsigned cm = lm | __reduce_or_sync(FULL, lost ? 1u << seen : 0u);
                     const bool inc = (cm >> lane) & 1u;
-                    if (act && !inc) acc[slot] = add_term<AR>(acc[slot], as, pr);
                     int rank = 0;
                     if (inc) rank = __popc(__match_any_sync(cm, slot) & lanemask_lt());
                     const int maxr = (int)__reduce_max_sync(FULL, (unsigned)rank);
-                    for (int rr = 0; rr <= maxr; rr++) {
+                    // round 0: the lanes that share no slot together with the first lane
+                    // of each shared slot (all their slots are distinct), then one round
+                    // per further lane of a shared slot
+                    if (act && rank == 0) acc[slot] = add_term<AR>(acc[slot], as, pr);
+                    __syncwarp();
+                    for (int rr = 1; rr <= maxr; rr++) {
                         if (inc && rank == rr) acc[slot] = add_term<AR>(acc[slot], as, pr);
                         __syncwarp();
                     }
