@@ -55,9 +55,12 @@ struct hsmu_handle_s {
     int *arena_col;
     TileEnt *arena_ent;
     long long arena_cap, arena_want;
-    // host-buffer entry: copy streams and their ordering events
+    // host-buffer entry: copy streams and their ordering events, and a page-locked
+    // array of the products per PROD_CHUNK rows (grown on demand) that orders the row panels
     cudaStream_t cs_in, cs_out;
     cudaEvent_t ev_in, ev_panel, ev_out;
+    long long *h_prod;
+    size_t h_prod_cap;
     // B's tile conversion runs on its own stream beside the bounds pass
     cudaStream_t cs_tiles;
     cudaEvent_t ev_tiles_start, ev_tiles_done;
@@ -82,10 +85,14 @@ const char *kErr[] = {"ok",
 // panel's compute (the copy back starts after it) or the last panel's copy.
 // A product whose output outruns the host link (more than HOST_LINK_BOUND
 // output bytes per intermediate product: the copy takes longer than the
-// compute) starts small and grows by HOST_PANEL_GROWTH to the middle, then
-// shrinks as much; one whose compute is the longer part only needs a small
+// compute) is cut into panels that grow by HOST_PANEL_GROWTH to the middle,
+// then shrink as much; one whose compute is the longer part only needs a small
 // last panel, and its sizes shrink by HOST_PANEL_RATIO from the first (small
 // panels leave the GPU partly idle, so only one end is made small).
+// The panels then run in the order that keeps the link busy soonest and
+// longest (panel_order): products per output entry differ by orders of
+// magnitude between rows (R-MAT's hub rows), so in row order the first panel
+// can hold many times its share of the compute.
 constexpr long long HOST_PANEL_BYTES = 32ll << 20;
 
 // entries of B from which its tile conversion runs on a second stream beside the bounds pass
@@ -248,6 +255,7 @@ struct PlainRun {
     bool tiles_aside = false;  // B's tiles are being built on the handle's conversion stream
     DevTiles Btd{};
     RowInfo ri{};
+    long long *chunk_prod = nullptr;  // products per PROD_CHUNK rows (host-buffer entry)
     int *scan_tmp = nullptr;
     Window *win = nullptr;
     long long win_cap = 0;
@@ -293,10 +301,11 @@ struct PlainRun {
     }
 
     // host_rp != NULL: the row pointers of C are copied there in the same host read
+    // host_prod != NULL: also the products of every PROD_CHUNK rows (ceil(M / PROD_CHUNK) entries)
     int symbolic(const hsmu_csr *B, const hsmu_btiles *Bt_in, bool count_tiles, int32_t *host_rp,
-                 cudaEvent_t ev_tiles) {
+                 cudaEvent_t ev_tiles, long long *host_prod = nullptr) {
         int rc = tiles_bounds(B, Bt_in, count_tiles, ev_tiles, o.no_tile_store == 0);
-        if (!rc) rc = count_scan(host_rp);
+        if (!rc) rc = count_scan(host_rp, host_prod);
         return rc;
     }
 
@@ -373,7 +382,7 @@ struct PlainRun {
 
     // exact count of every row (the large rows' tiles kept in the arena while it lasts),
     // scan into C's row pointers and nnz(C), one host read
-    int count_scan(int32_t *host_rp) {
+    int count_scan(int32_t *host_rp, long long *host_prod = nullptr) {
         CKR(palloc(&crp, (size_t)M + 1, st));
         launch_count_small(Ad, Bd, Btd, ri, ctl, h->nsm, st);
         const TileStore tsd = store_view();
@@ -390,6 +399,13 @@ struct PlainRun {
         CKR(cudaGetLastError());
         CKR(cudaMemcpyAsync(h->h_ctl, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
         if (host_rp) CKR(cudaMemcpyAsync(host_rp, crp, sizeof(int32_t) * ((size_t)M + 1), cudaMemcpyDeviceToHost, st));
+        if (host_prod && M > 0) {
+            const size_t nch = ((size_t)M + PROD_CHUNK - 1) / PROD_CHUNK;
+            CKR(palloc(&chunk_prod, nch, st));
+            launch_chunk_prod(M, ri.prod, chunk_prod, grid_rows(h), st);
+            launches++;
+            CKR(cudaMemcpyAsync(host_prod, chunk_prod, sizeof(long long) * nch, cudaMemcpyDeviceToHost, st));
+        }
         CKR(cudaStreamSynchronize(st));
         hc = *h->h_ctl;
         if (ri.store && hc.store_tiles > h->arena_want) h->arena_want = hc.store_tiles;  // for the next call
@@ -474,6 +490,7 @@ struct PlainRun {
             own_tiles = false;
         }
         pfree(ri.prod, st);
+        pfree(chunk_prod, st);
         pfree(ri.tmin, st);
         pfree(ri.tmax, st);
         pfree(ri.bins, st);
@@ -578,6 +595,42 @@ int spgemm_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, const hs
 // 2.8x slower than this on GB300: the fused kernel's row-sized writes go out
 // over the CPU link at a fraction of its copy bandwidth.)
 // The result is the same as hsmu_spgemm followed by a download.
+// Order of the row panels (cut: np + 1 row bounds; rp: C's row pointers on the host):
+// the order of a two-stage flow shop (compute, then the copy back) that ends first,
+// by S. M. Johnson's rule (1954) -- panels whose copy is the longer part first, by
+// increasing compute, then the others by decreasing copy.  A panel's compute is
+// counted in intermediate products (chunk: the products of every PROD_CHUNK rows,
+// a chunk cut by a panel bound shared by row count; nullable: row order), its copy
+// in output bytes / HOST_LINK_BOUND.
+std::vector<int> panel_order(const std::vector<int> &cut, const int32_t *rp, const long long *chunk, int M) {
+    const int np = (int)cut.size() - 1;
+    std::vector<int> order((size_t)np);
+    for (int q = 0; q < np; q++) order[(size_t)q] = q;
+    if (!chunk || np < 2) return order;
+    // products of rows [0, r): whole chunks, then the share of the chunk that r cuts
+    auto before = [&](int r, long long &c_at, double &acc_at) -> double {
+        const long long c = r / PROD_CHUNK;
+        for (; c_at < c; c_at++) acc_at += (double)chunk[c_at];
+        const int rows = (int)std::min<long long>(PROD_CHUNK, (long long)M - c * PROD_CHUNK);
+        return acc_at + (r % PROD_CHUNK && rows > 0 ? (double)chunk[c] * (r % PROD_CHUNK) / rows : 0.0);
+    };
+    std::vector<double> comp((size_t)np), copy((size_t)np);
+    long long c_at = 0;
+    double acc_at = 0.0, prev = 0.0;
+    for (int q = 0; q < np; q++) {
+        const double upto = before(cut[(size_t)q + 1], c_at, acc_at);
+        comp[(size_t)q] = upto - prev;
+        prev = upto;
+        copy[(size_t)q] = 12.0 * (double)(rp[cut[(size_t)q + 1]] - rp[cut[(size_t)q]]) / HOST_LINK_BOUND;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const bool la = comp[(size_t)a] < copy[(size_t)a], lb = comp[(size_t)b] < copy[(size_t)b];
+        if (la != lb) return la;
+        return la ? comp[(size_t)a] < comp[(size_t)b] : copy[(size_t)a] > copy[(size_t)b];
+    });
+    return order;
+}
+
 int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_opts *opts,
                      cudaStream_t st, hsmu_stats *stats) {
     if (!h || !csr_ok(A) || !csr_ok(B) || !C || !C->row_ptr) return HSMU_ERR_INVALID;
@@ -615,6 +668,19 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
             CKR(cudaMemcpyAsync(D->val, X->val, sizeof(double) * (size_t)X->nnz, cudaMemcpyHostToDevice, h->cs_in));
         return HSMU_OK;
     };
+    // products per PROD_CHUNK rows, read with the row pointers, order the panels
+    // (page-locked, kept by the handle; without it the panels run in row order)
+    const size_t nchunk = ((size_t)M + PROD_CHUNK - 1) / PROD_CHUNK;
+    if (nchunk > 0 && h->h_prod_cap < nchunk) {
+        if (h->h_prod) cudaFreeHost(h->h_prod);
+        h->h_prod = nullptr;
+        h->h_prod_cap = 0;
+        if (cudaMallocHost(reinterpret_cast<void **>(&h->h_prod), sizeof(long long) * nchunk) == cudaSuccess)
+            h->h_prod_cap = nchunk;
+        else
+            h->h_prod = nullptr, (void)cudaGetLastError();
+    }
+    long long *host_prod = nchunk > 0 && h->h_prod_cap >= nchunk ? h->h_prod : nullptr;
     std::vector<int> cut;
     r.reserve_windows = false;  // the output is written in row panels
     rc = upload(B, &dB);
@@ -624,7 +690,7 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
     }
     if (!rc) CK(cudaEventRecord(h->ev_in, h->cs_in));
     if (!rc) rc = r.begin(&dA, &dB);
-    if (!rc) rc = r.symbolic(&dB, nullptr, stats != nullptr, C->row_ptr, stats ? h->ev[1] : nullptr);
+    if (!rc) rc = r.symbolic(&dB, nullptr, stats != nullptr, C->row_ptr, stats ? h->ev[1] : nullptr, host_prod);
     if (!rc && stats) cudaEventRecord(h->ev[2], st);
     if (!rc && r.hc.nnz > capacity) {
         // report the size; the row pointers are already in C->row_ptr
@@ -658,21 +724,30 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
             cut.push_back(row < cut.back() ? cut.back() : (row > M ? M : row));
         }
         cut.push_back(M);
-        for (size_t q = 0; q + 1 < cut.size(); q++) {
+        const std::vector<int> order = panel_order(cut, C->row_ptr, host_prod, M);
+        bool first = true;
+        for (const int q : order) {
             const int lo = cut[q], hi = cut[q + 1];
             if (lo == hi) continue;
-            if (q > 0) {
+            if (!first) {
                 rc = r.next_panel();
                 if (rc) break;
             }
-            r.structure(lo, hi);
-            r.values();
+            first = false;
             const long long e0 = C->row_ptr[lo], e1 = C->row_ptr[hi];
+            // the columns are final after the structure pass: their copy starts while the
+            // value pass runs
+            r.structure(lo, hi);
+            if (e1 > e0) {
+                CK(cudaEventRecord(h->ev_panel, st));
+                CK(cudaStreamWaitEvent(h->cs_out, h->ev_panel, 0));
+                CK(cudaMemcpyAsync(C->col + e0, r.ccol + e0, sizeof(int32_t) * (size_t)(e1 - e0),
+                                   cudaMemcpyDeviceToHost, h->cs_out));
+            }
+            r.values();
             if (e1 == e0) continue;
             CK(cudaEventRecord(h->ev_panel, st));
             CK(cudaStreamWaitEvent(h->cs_out, h->ev_panel, 0));
-            CK(cudaMemcpyAsync(C->col + e0, r.ccol + e0, sizeof(int32_t) * (size_t)(e1 - e0), cudaMemcpyDeviceToHost,
-                               h->cs_out));
             CK(cudaMemcpyAsync(C->val + e0, r.cval + e0, sizeof(double) * (size_t)(e1 - e0), cudaMemcpyDeviceToHost,
                                h->cs_out));
         }
@@ -1186,6 +1261,7 @@ int hsmu_handle_destroy(hsmu_handle h) {
     for (cudaStream_t s : {h->cs_in, h->cs_out, h->cs_tiles})
         if (s) cudaStreamDestroy(s);
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
+    if (h->h_prod) cudaFreeHost(h->h_prod);
     delete h;
     return HSMU_OK;
 }

@@ -92,6 +92,9 @@ void launch_validate(const DevCSR &A, Ctl *ctl, int grid, cudaStream_t st);
 
 // k_rows.cu
 void launch_bounds(const DevCSR &A, const DevCSR &B, RowInfo ri, Ctl *ctl, int grid, int *scan_tmp, cudaStream_t st);
+// out[c] = products of rows c*PROD_CHUNK .. (c+1)*PROD_CHUNK-1 (ceil(M / PROD_CHUNK) entries)
+constexpr int PROD_CHUNK = 64;
+void launch_chunk_prod(int M, const long long *prod, long long *out, int grid, cudaStream_t st);
 // exclusive scan of int counts (n entries) into out[0..n]; total (int64) into *total64;
 // sets DERR_OVERFLOW if the total exceeds INT32_MAX.  tmp must hold scan_tmp_ints(n) ints.
 // in == out (an in-place scan) is allowed.

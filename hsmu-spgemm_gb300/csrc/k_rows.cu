@@ -155,6 +155,25 @@ void launch_bounds(const DevCSR &A, const DevCSR &B, RowInfo ri, Ctl *ctl, int g
     k_bin_emit<<<grid, 256, 0, st>>>(A.M, ri.cls, off, ri.bins);
 }
 
+// products of every PROD_CHUNK consecutive rows: one warp per chunk (the host
+// orders its row panels by them)
+__global__ void __launch_bounds__(256) k_chunk_prod(int M, const long long *__restrict__ prod,
+                                                    long long *__restrict__ out) {
+    static_assert(PROD_CHUNK == 2 * WARP, "two rows per lane");
+    const int nch = (M + PROD_CHUNK - 1) / PROD_CHUNK;
+    const int lane = lane_id();
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nch; c += (gridDim.x * blockDim.x) >> 5) {
+        const int r0 = c * PROD_CHUNK + lane, r1 = r0 + WARP;
+        long long v = (r0 < M ? prod[r0] : 0ll) + (r1 < M ? prod[r1] : 0ll);
+        v = warp_sum(v);
+        if (lane == 0) out[c] = v;
+    }
+}
+
+void launch_chunk_prod(int M, const long long *prod, long long *out, int grid, cudaStream_t st) {
+    if (M > 0) k_chunk_prod<<<grid, 256, 0, st>>>(M, prod, out);
+}
+
 // ---------------------------------------------------------------- scan
 constexpr int SCAN_T = 256;
 constexpr int SCAN_IPT = 8;

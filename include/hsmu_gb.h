@@ -102,7 +102,8 @@ typedef struct hsmu_opts {
                            * of output; at most 8).  Sizes shrink from the first panel when the
                            * compute takes longer than the copy back; when the copy is the longer
                            * part they double from the first panel to the middle and halve
-                           * towards the last */
+                           * towards the last.  The panels run in the order that keeps the host
+                           * link busy soonest (the least compute first) */
     int32_t wait_polls;   /* test hook, 0 in normal use.  > 0: every bounded device wait of the call
                            * gives up after this many polls instead of its default limit (the value
                            * pass's wait for a window's column copy polls without blocking; the batch's
