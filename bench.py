@@ -444,7 +444,26 @@ def measure_plain(eng, A, B, name, steps, warmup, arith, world=1, rank=0, local=
     def e2e_step():
         eng.spgemm_host(hA, hB, out=oC, arith=ar, stream=stream)
 
+    # the host link is shared with the machine's other jobs: a plain copy of the same
+    # output bytes into the same page-locked arrays, just before and just after the
+    # timed calls, records what it gave during them
+    def link_copy_ms():
+        d_col = torch.empty(oC[1].shape, dtype=oC[1].dtype, device=stream.device)
+        d_val = torch.empty(oC[2].shape, dtype=oC[2].dtype, device=stream.device)
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        c0.record(stream)
+        with torch.cuda.stream(stream):
+            oC[1].copy_(d_col, non_blocking=True)
+            oC[2].copy_(d_val, non_blocking=True)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        del d_col, d_val
+        return c0.elapsed_time(c1)
+
     e2e_step()
+    link_before = link_copy_ms()
     torch.cuda.synchronize()
     dist_barrier(world)
     e0 = torch.cuda.Event(enable_timing=True)
@@ -455,8 +474,10 @@ def measure_plain(eng, A, B, name, steps, warmup, arith, world=1, rank=0, local=
         e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
+    link_after = link_copy_ms()
     e2e_ms = dist_max(e0.elapsed_time(e1) / ke, world)
     e2e_value = 2.0 * products_total / (e2e_ms * 1e-3) / 1e9
+    link_bytes = oC[1].numel() * oC[1].element_size() + oC[2].numel() * oC[2].element_size()
     del hA, hB, oC
 
     # ---- roofline of the dominant kernel.  Values are accumulated either in the
@@ -489,7 +510,11 @@ def measure_plain(eng, A, B, name, steps, warmup, arith, world=1, rank=0, local=
                      "gather_gbs": round(gather_bytes / (kms * 1e-3) / 1e9, 2)},
         "fp64_ops": fp64_per_product * products_mine, "kernel_ms": kms,
         "e2e": {"value": round(e2e_value, 3), "unit": "GFLOPS", "ms_per_step": round(e2e_ms, 4),
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "link": {"note": "plain copy of C's columns and values over the host link, just before / "
+                                 "after the timed calls",
+                         "ms": [round(link_before, 2), round(link_after, 2)],
+                         "gbs": [round(link_bytes / (t * 1e-3) / 1e9, 1) for t in (link_before, link_after)]}},
         "clocks": clk,
     }
 
