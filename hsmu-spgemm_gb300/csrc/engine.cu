@@ -434,8 +434,9 @@ struct PlainRun {
         wc.cap = cap;
         CKR(palloc(&wc.len, (size_t)nwin, st));
         CKR(palloc(&wc.off, (size_t)nwin + 1, st));
-        CKR(palloc(&wc.total, 1, st));
+        CKR(palloc(&wc.total, 2, st));
         CKR(palloc(&wc.scan_tmp, scan_tmp_ints((int)nwin), st));
+        CKR(palloc(&wc.item_off, (size_t)nwin + 1, st));
         CKR(palloc(&wc.cur, (size_t)cap, st));
         return HSMU_OK;
     }
@@ -462,7 +463,7 @@ struct PlainRun {
         const TileStore tsd = store_view();
         launch_numeric(Ad, Bd, Btd, crp, ccol, cval, win, win_cap, nullptr, nullptr, nullptr, wc, ctl, o.arith, h->nsm,
                        st, o.wait_polls, have_store ? &tsd : nullptr);
-        launches += 6;  // window lengths, 3 scan, cursors, values
+        launches += 9;  // window lengths, two scans of 3, cursors, values
     }
 
     // start a new panel: its windows reuse the window buffer from slot 0
@@ -508,6 +509,7 @@ struct PlainRun {
         pfree(wc.off, st);
         pfree(wc.total, st);
         pfree(wc.scan_tmp, st);
+        pfree(wc.item_off, st);
         pfree(wc.cur, st);
         pfree(crp, st);
         if (ext_col) {
@@ -930,8 +932,9 @@ learned:
             wc.cap = cur_cap;
             CK(palloc(&wc.len, (size_t)win_cap, st));
             CK(palloc(&wc.off, (size_t)win_cap + 1, st));
-            CK(palloc(&wc.total, 1, st));
+            CK(palloc(&wc.total, 2, st));
             CK(palloc(&wc.scan_tmp, scan_tmp_ints((int)win_cap), st));
+            CK(palloc(&wc.item_off, (size_t)win_cap + 1, st));
             CK(palloc(&wc.cur, (size_t)cur_cap, st));
         }
         if (stats) cudaEventRecord(h->ev[3], st);
@@ -1040,6 +1043,7 @@ done:
     pfree(wc.off, st);
     pfree(wc.total, st);
     pfree(wc.scan_tmp, st);
+    pfree(wc.item_off, st);
     pfree(wc.cur, st);
     pfree(crp, st);
     pfree(ccol, st);

@@ -141,13 +141,14 @@ void launch_structure(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, RowI
 // flag (nullable): speculative-pass windows of rows flagged ROW_OVERFLOW are skipped;
 // scol/soff (nullable): speculative slots holding the columns of speculative-pass
 // windows, which the kernel copies to ccol
-// per-window cursors into the B rows (k_win_cursors): len/off/scan_tmp sized for
-// win_cap windows (+1), cur for cap entries (Ctl::cur_bound)
+// per-window cursors into the B rows (k_win_cursors): len/off/item_off/scan_tmp sized
+// for win_cap windows (+1), total for 2 entries, cur for cap entries (Ctl::cur_bound)
 struct WinCursors {
     int *len;
     long long *off;
     long long *total;
     int *scan_tmp;
+    int *item_off;  // the cursor pass's work items per window, scanned in place
     int *cur;
     long long cap;
 };

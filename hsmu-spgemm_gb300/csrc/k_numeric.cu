@@ -17,9 +17,10 @@
 // span with per-word prefix counts gives the tile's rank r, which then
 // indexes tmask/tbase:  r = opre[t >> 6] + popc(occ[t >> 6] below bit t & 63).
 // Where each B row enters a window is precomputed for every (window, A entry)
-// pair by k_win_cursors, a search per pair run with all pairs in flight at
-// once; the window kernel reads its segment [cursor(w), cursor(w+1)) with two
-// loads instead of searching B rows inside its latency-bound loop.
+// pair by k_win_cursors -- one search per chunk of consecutive windows of a
+// row, then a short forward search per window -- so the window kernel reads
+// its segment [cursor(w), cursor(w+1)) with two loads instead of searching B
+// rows inside its latency-bound loop.
 //
 // Accumulation order is deterministic and equals the oracle's: the products
 // of the window are walked in the flat order (A entry, then B entry), 32 per
@@ -62,26 +63,39 @@ struct alignas(16) NumSmem {
 static_assert(NUM_CTAS_PER_SM * (NUM_WARPS * sizeof(NumSmem) + 1024) <= 228 * 1024, "CTAs per SM");
 static_assert(WIN_CAP * 8 >= (WIN_CAP + 8) * 4, "column stage fits in the accumulator");
 
+// The cursor pass works on chunks: runs of at most CUR_CHUNK consecutive
+// windows of one row whose first tiles ascend, aligned to multiples of
+// CUR_CHUNK in the window array.  Window w continues the chunk of w - 1 when:
+constexpr int CUR_CHUNK = 16;
+__device__ __forceinline__ bool cur_continues(const Window *win, int w, int row, int t0) {
+    return w % CUR_CHUNK != 0 && win[w - 1].row == row && win[w - 1].t0 < t0;
+}
+
 // A entries of each window's row (0 past the emitted windows), scanned into
-// the windows' offsets in the cursor array.  A window written with a slot
+// the windows' offsets in the cursor array, and the cursor pass's work items
+// (CUR_CHUNK).  A window written with a slot
 // count of 0 (the large rows built from their stored tiles) gets its count
 // here: up to the next window's first slot when that window continues the
 // same row, else up to the row's end; and its tile count likewise, up to the
 // next window's first tile or the end of the row's list.
 __global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int win_cap, int M, const int *__restrict__ arp,
                                                  const int *__restrict__ crp, const long long *__restrict__ ts_off,
-                                                 const int *__restrict__ ts_cnt, Ctl *ctl, int *__restrict__ len) {
+                                                 const int *__restrict__ ts_cnt, Ctl *ctl, int *__restrict__ len,
+                                                 int *__restrict__ items) {
     const int nwin = min(ctl->win_count, win_cap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < win_cap; w += gridDim.x * blockDim.x) {
-        int n = 0;
+        int n = 0, it = 0;
         if (w < nwin) {
             const int row = win[w].row;
             if ((unsigned)row >= (unsigned)M) {  // a window left unwritten after a reported error
                 set_err(&ctl->err, DERR_INTERNAL);
                 len[w] = 0;
+                items[w] = 0;
                 continue;
             }
             n = arp[row + 1] - arp[row];
+            // a chunk of the cursor pass starts here: one work item per 32 A entries
+            if (!cur_continues(win, w, row, win[w].t0)) it = (n + WARP - 1) / WARP;
             if (win[w].cnt == 0) {
                 const int s0 = win[w].s0, li = win[w].li;
                 int e = crp[row + 1] - crp[row];
@@ -96,41 +110,84 @@ __global__ void __launch_bounds__(256) k_win_len(Window *__restrict__ win, int w
             }
         }
         len[w] = n;
+        items[w] = it;
     }
+}
+
+// largest index w in [0, n] with a[w] <= x, for non-decreasing a with a[0] <= x:
+// all 32 lanes probe 32 evenly spaced entries per round (log32(n) rounds)
+__device__ __forceinline__ int warp_last_le(const int *__restrict__ a, int n, int x) {
+    const int lane = lane_id();
+    int lo = 0, hi = n;  // the answer lies in [lo, hi]; a[lo] <= x
+    while (hi > lo) {
+        const int step = (hi - lo + WARP - 1) / WARP;
+        const int p = lo + (lane + 1) * step;
+        const bool le = p <= hi && a[p] <= x;
+        const int c = __popc(__ballot_sync(FULL, le));  // probes that hold form a prefix
+        const int nhi = min(hi, lo + (c + 1) * step - 1);
+        lo += c * step;
+        hi = nhi;
+    }
+    return lo;
 }
 
 // cursor of (window w, A entry p of its row): index of the first entry of B row
 // acol[p] whose column lies in or after the window's first tile -- found in
-// B's sorted tile list, whose tile_off gives the tile's first entry.  One warp
-// per window, all pairs in flight at once.  (Seeding each window's search from
-// the previous window of the same row -- a warp taking 8 consecutive windows,
-// one binary search and then forward gallops per A entry -- was measured
-// slower: R-MAT 18 value stage 28.1 -> 30.4 ms, the chained gallops of a heavy
-// row's group form a tail and fewer searches run at once.)
+// B's sorted tile list, whose tile_off gives the tile's first entry.  A work
+// item is one chunk of windows (CUR_CHUNK) and 32 A entries of its row, a lane
+// per entry: a binary search for the chunk's first window, then, as the
+// windows' first tiles ascend, a forward search from the previous position for
+// each further window (mostly a probe or two in the same cache lines).  Every
+// warp takes an equal share of the items (item_off: the items scanned over the
+// windows), finding its first by one warp-wide search.  (A search per pair,
+// all pairs in flight, took 4.6 ms of R-MAT 18's 23.8 ms value stage: its
+// heavy rows pair thousands of A entries, many of them long B rows, with
+// hundreds of windows.  Seeding each window's search from the previous window
+// with whole rows per warp was slower still: the chained searches of a heavy
+// row formed a tail.)
 __global__ void __launch_bounds__(256) k_win_cursors(const Window *__restrict__ win, int win_cap, int M,
                                                      const long long *__restrict__ woff, long long cur_cap,
                                                      const int *__restrict__ arp, const int *__restrict__ acol,
                                                      const int *__restrict__ brp, const int *__restrict__ tptr,
                                                      const int *__restrict__ tcol, const int *__restrict__ toff,
-                                                     int *__restrict__ wcur, Ctl *ctl) {
+                                                     const int *__restrict__ item_off, int *__restrict__ wcur,
+                                                     Ctl *ctl) {
     const int nwin = min(ctl->win_count, win_cap);
     const int lane = lane_id();
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int w = gw; w < nwin; w += nw) {
+    const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long total = item_off[nwin];
+    const int i0 = (int)(total * gw / nw), i1 = (int)(total * (gw + 1) / nw);
+    if (i0 >= i1) return;
+    int w = warp_last_le(item_off, nwin, i0);
+    for (int i = i0; i < i1; i++) {
+        while (item_off[w + 1] <= i) w++;  // windows inside the previous chunk have no items
         const Window W = win[w];
-        if ((unsigned)W.row >= (unsigned)M) continue;  // reported by k_win_len
-        const int a_lo = arp[W.row], a_hi = arp[W.row + 1];
-        const long long base = woff[w];
-        if (base + (a_hi - a_lo) > cur_cap) {
-            if (lane == 0) set_err(&ctl->err, DERR_CAPACITY);
-            continue;
-        }
-        for (int p = a_lo + lane; p < a_hi; p += WARP) {
+        const int row = W.row;
+        if ((unsigned)row >= (unsigned)M) continue;  // reported by k_win_len
+        const int a_lo = arp[row], a_hi = arp[row + 1];
+        const int p = a_lo + (i - item_off[w]) * WARP + lane;
+        const bool v = p < a_hi;
+        int lo = 0, hi = 0, bend = 0;
+        if (v) {
             const int k = __ldg(acol + p);
-            const int lo = __ldg(tptr + k), hi = __ldg(tptr + k + 1);
-            const int idx = lower_bound_i32(tcol, lo, hi, W.t0);
-            wcur[base + (p - a_lo)] = idx < hi ? __ldg(toff + idx) : __ldg(brp + k + 1);
+            lo = __ldg(tptr + k);
+            hi = __ldg(tptr + k + 1);
+            bend = __ldg(brp + k + 1);
+        }
+        int idx = v ? lower_bound_i32(tcol, lo, hi, W.t0) : 0;
+        for (int ww = w;;) {
+            const long long base = woff[ww];
+            if (base + (a_hi - a_lo) > cur_cap) {
+                if (lane == 0) set_err(&ctl->err, DERR_CAPACITY);
+            } else if (v) {
+                wcur[base + (p - a_lo)] = idx < hi ? __ldg(toff + idx) : bend;
+            }
+            if (++ww >= nwin) break;
+            const Window W2 = win[ww];
+            if (!cur_continues(win, ww, W2.row, W2.t0)) break;  // W2.row == row when it continues
+            const int t0 = W2.t0;
+            if (v) idx = gallop_gt(tcol, idx, hi, t0 - 1);  // first tile >= t0
         }
     }
 }
@@ -397,10 +454,11 @@ void launch_numeric(const DevCSR &A, const DevCSR &B, const DevTiles &Bt, const 
     if (win_cap <= 0) return;
     cudaMemsetAsync(&ctl->win_next, 0, sizeof(int), st);
     k_win_len<<<nsm * 4, 256, 0, st>>>(const_cast<Window *>(win), (int)win_cap, A.M, A.rp, crp, ts ? ts->off : nullptr,
-                                       ts ? ts->cnt : nullptr, ctl, wc.len);
+                                       ts ? ts->cnt : nullptr, ctl, wc.len, wc.item_off);
     launch_scan64(wc.len, wc.off, (int)win_cap, wc.total, wc.scan_tmp, st);
+    launch_scan(wc.item_off, wc.item_off, (int)win_cap, wc.total + 1, wc.scan_tmp, ctl, st);
     k_win_cursors<<<nsm * 16, 256, 0, st>>>(win, (int)win_cap, A.M, wc.off, wc.cap, A.rp, A.col, B.rp, Bt.ptr, Bt.col,
-                                            Bt.off, wc.cur, ctl);
+                                            Bt.off, wc.item_off, wc.cur, ctl);
     auto k = arith == AR_IMUL ? k_numeric<AR_IMUL> : arith == AR_FMA ? k_numeric<AR_FMA> : k_numeric<AR_RN>;
     k<<<nsm * NUM_CTAS_PER_SM, NUM_WARPS * 32, NUM_WARPS * sizeof(NumSmem), st>>>(
         A.rp, A.col, A.val, B.rp, B.col, B.val, crp, ccol, cval, win, (int)win_cap, flag, scol, soff, wc.off, wc.cur,
