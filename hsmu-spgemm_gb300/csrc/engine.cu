@@ -633,6 +633,35 @@ std::vector<int> panel_order(const std::vector<int> &cut, const int32_t *rp, con
     return order;
 }
 
+// The host-buffer call's row panels: cut (np + 1 row bounds, panel q = rows
+// [cut[q], cut[q+1]), each ending at the first row whose entries start at or
+// after the panel's share of nnz) and the order they run in (panel_order).
+// rp: C's row pointers (M + 1); products: the product's intermediate products;
+// chunk: products per PROD_CHUNK rows (nullable); panels: hsmu_opts.panels.
+void plan_panels(int M, const int32_t *rp, long long products, const long long *chunk, int panels,
+                 std::vector<int> &cut, std::vector<int> &order) {
+    const long long nnz = rp[M];
+    long long np = panels > 0 ? panels : (nnz * 12 + HOST_PANEL_BYTES - 1) / HOST_PANEL_BYTES;
+    np = np < 1 ? 1 : (np > HOST_MAX_PANELS ? HOST_MAX_PANELS : np);
+    if (np > M) np = M > 0 ? M : 1;
+    cut.assign(1, 0);
+    const bool link_bound = 12.0 * (double)nnz > HOST_LINK_BOUND * (double)products;
+    std::vector<double> share((size_t)np);
+    double wsum = 0.0;
+    for (long long q = 0; q < np; q++)
+        wsum += (share[q] = link_bound ? std::pow(HOST_PANEL_GROWTH, (double)std::min(q, np - 1 - q))
+                                       : std::pow(HOST_PANEL_RATIO, (double)q));
+    double acc = 0.0;
+    for (long long q = 1; q < np; q++) {
+        acc += share[q - 1];
+        const long long target = (long long)((double)nnz * (acc / wsum));
+        const int row = (int)(std::lower_bound(rp, rp + M + 1, (int32_t)target) - rp);
+        cut.push_back(row < cut.back() ? cut.back() : (row > M ? M : row));
+    }
+    cut.push_back(M);
+    order = panel_order(cut, rp, chunk, M);
+}
+
 int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsmu_csr *C, const hsmu_opts *opts,
                      cudaStream_t st, hsmu_stats *stats) {
     if (!h || !csr_ok(A) || !csr_ok(B) || !C || !C->row_ptr) return HSMU_ERR_INVALID;
@@ -705,28 +734,8 @@ int spgemm_host_impl(hsmu_handle_s *h, const hsmu_csr *A, const hsmu_csr *B, hsm
     if (!rc) {
         if (stats) cudaEventRecord(h->ev[3], st);
         CK(cudaStreamWaitEvent(st, h->ev_in, 0));  // values of A and B are on the device
-        const long long nnz = r.hc.nnz;
-        long long np = o.panels > 0 ? o.panels : (nnz * 12 + HOST_PANEL_BYTES - 1) / HOST_PANEL_BYTES;
-        np = np < 1 ? 1 : (np > HOST_MAX_PANELS ? HOST_MAX_PANELS : np);
-        if (np > M) np = M > 0 ? M : 1;
-        // panel q = rows [cut[q], cut[q+1]): the first row whose entries start at or after the
-        // panel's share of nnz
-        cut.push_back(0);
-        const bool link_bound = 12.0 * (double)nnz > HOST_LINK_BOUND * (double)r.hc.products;
-        std::vector<double> share((size_t)np);
-        double wsum = 0.0;
-        for (long long q = 0; q < np; q++)
-            wsum += (share[q] = link_bound ? std::pow(HOST_PANEL_GROWTH, (double)std::min(q, np - 1 - q))
-                                           : std::pow(HOST_PANEL_RATIO, (double)q));
-        double acc = 0.0;
-        for (long long q = 1; q < np; q++) {
-            acc += share[q - 1];
-            const long long target = (long long)((double)nnz * (acc / wsum));
-            const int row = (int)(std::lower_bound(C->row_ptr, C->row_ptr + M + 1, (int32_t)target) - C->row_ptr);
-            cut.push_back(row < cut.back() ? cut.back() : (row > M ? M : row));
-        }
-        cut.push_back(M);
-        const std::vector<int> order = panel_order(cut, C->row_ptr, host_prod, M);
+        std::vector<int> order;
+        plan_panels(M, C->row_ptr, (long long)r.hc.products, host_prod, o.panels, cut, order);
         bool first = true;
         for (const int q : order) {
             const int lo = cut[q], hi = cut[q + 1];
@@ -1416,6 +1425,18 @@ int hsmu_selftest_dmul(uint64_t n, uint64_t seed, uint64_t *mismatches, void *st
 int hsmu_debug_fail_alloc(int64_t nth) {
     if (nth < 0) return HSMU_ERR_INVALID;
     g_fail_alloc_countdown.store((long long)nth, std::memory_order_relaxed);
+    return HSMU_OK;
+}
+
+int hsmu_debug_plan_panels(int32_t M, const int32_t *row_ptr, int64_t products, const int64_t *chunk_products,
+                           int32_t panels, int32_t *n_panels, int32_t *cut, int32_t *order) {
+    if (M < 0 || !row_ptr || panels < 0 || !n_panels || !cut || !order) return HSMU_ERR_INVALID;
+    static_assert(sizeof(long long) == sizeof(int64_t), "chunk products");
+    std::vector<int> c, ord;
+    plan_panels(M, row_ptr, (long long)products, reinterpret_cast<const long long *>(chunk_products), panels, c, ord);
+    *n_panels = (int32_t)ord.size();
+    for (size_t q = 0; q < c.size(); q++) cut[q] = c[q];
+    for (size_t q = 0; q < ord.size(); q++) order[q] = ord[q];
     return HSMU_OK;
 }
 

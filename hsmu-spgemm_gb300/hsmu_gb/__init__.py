@@ -43,7 +43,8 @@ EXPORTS = ["hsmu_strerror", "hsmu_abi_version", "hsmu_handle_create", "hsmu_hand
            "hsmu_batch_result", "hsmu_batch_set_params", "hsmu_batch_autotune", "hsmu_batch_destroy",
            "hsmu_gen_poisson7", "hsmu_gen_aggregation", "hsmu_spgemm_learned", "hsmu_row_features",
            "hsmu_row_nnz", "hsmu_mlp_forward", "hsmu_mlp_grad", "hsmu_mlp_adam", "hsmu_spgemm64",
-           "hsmu_csr64_free", "hsmu_csr64_download", "hsmu_probe_fp64_rate", "hsmu_debug_fail_alloc"]
+           "hsmu_csr64_free", "hsmu_csr64_download", "hsmu_probe_fp64_rate", "hsmu_debug_fail_alloc",
+           "hsmu_debug_plan_panels"]
 MLP_FLOATS = 1259
 
 
@@ -149,6 +150,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     L.hsmu_selftest_dmul.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), P]
     L.hsmu_probe_fp64_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), P]
     L.hsmu_debug_fail_alloc.argtypes = [ctypes.c_int64]
+    L.hsmu_debug_plan_panels.argtypes = [ctypes.c_int32, P, ctypes.c_int64, P, ctypes.c_int32, P, P, P]
     L.hsmu_spgemm64.argtypes = [P, ctypes.POINTER(c_csr), ctypes.POINTER(c_csr), ctypes.POINTER(c_csr64),
                                 ctypes.c_int64, ctypes.POINTER(c_opts), P]
     L.hsmu_csr64_free.argtypes = [ctypes.POINTER(c_csr64)]

@@ -336,6 +336,18 @@ int hsmu_probe_fp64_rate(int iters, double *lane_ops_per_s, void *stream);
  * inc/cuda_comm.h:16-29). */
 int hsmu_debug_fail_alloc(int64_t nth);
 
+/* Test hook: the row panels hsmu_spgemm_host would use for a product with C's
+ * row pointers row_ptr (M + 1 entries), `products` intermediate products,
+ * chunk_products[c] = the products of rows 64c .. 64c+63 (ceil(M / 64)
+ * entries; NULL: the panels run in row order) and hsmu_opts.panels = panels.
+ * Writes the number of panels np (at most 8) to *n_panels, their row bounds
+ * to cut[0..np] (panel q = rows cut[q] .. cut[q+1]-1) and the order they run
+ * in to order[0..np-1]; cut needs 9 entries, order 8.  Host-only: no device
+ * call.  No reference counterpart (the reference computes C whole in one
+ * NHC_spgemm call, src/test.cu:71). */
+int hsmu_debug_plan_panels(int32_t M, const int32_t *row_ptr, int64_t products, const int64_t *chunk_products,
+                           int32_t panels, int32_t *n_panels, int32_t *cut, int32_t *order);
+
 #ifdef __cplusplus
 }
 #endif
