@@ -1037,8 +1037,8 @@ learned:
         cudaEventElapsedTime(&t, h->ev[0], h->ev[5]);
         stats->ms_total = t;
         // tiles 5, bounds + binning 6, features 1, capacity 1, scan 3, structure 3, scan 3, compact 1, redo 3,
-        // window cursors 5, numeric 1
-        stats->launches = (o.validate ? 2 : 0) + (win_cap > 0 ? 32 : 27);
+        // window lengths 1, their two scans 6, cursors 1, numeric 1
+        stats->launches = (o.validate ? 2 : 0) + (win_cap > 0 ? 35 : 27);
     }
 done:
     pfree(feat, st);
