@@ -83,9 +83,9 @@ TRAFFIC = {
     # profiles/k_struct_ds_stencil27_32_dof3.md: 445.5 MB on the 32^3 case, scaled by the
     # algorithmic bytes (x1.993) to the 40^3 workload
     "stencil27_40_dof3_AA": 887.9e6,
-    # profiles/k_numeric_rmat16_AA.md: 1.831 GB on R-MAT scale 16, scaled by the algorithmic
+    # profiles/k_numeric_rmat16_AA.md: 1.828 GB on R-MAT scale 16, scaled by the algorithmic
     # bytes (x7.765) to scale 18
-    "rmat18_AA": 14.22e9,
+    "rmat18_AA": 14.19e9,
     # profiles/k_batch_amg32_galerkin.md: 3.12 GB per launch of the 32-product batch (tuned
     # launch); the 512-product batch scaled by its algorithmic bytes (x11.82)
     "amg32_galerkin": 3.12e9,
