@@ -460,6 +460,7 @@ def measure_plain(eng, A, B, name, steps, warmup, arith, world=1, rank=0, local=
         c1.record(stream)
         torch.cuda.synchronize()
         del d_col, d_val
+        torch.cuda.empty_cache()  # the engine's own pool serves the configs that follow
         return c0.elapsed_time(c1)
 
     e2e_step()
